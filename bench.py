@@ -1,0 +1,336 @@
+"""Benchmark of the FDTD hot path on GB300.
+
+Default workload (the headline): the 2D TM PML benchmark program -- 8192x8192
+grid, 32-cell PML with cubic grading 0.333, lossy dielectric cylinder of radius
+1000 cells (eps_r=30, sigma=0.3 S/m), hard Gaussian Dz source at the centre
+(t0=20, spread=6), 2000 time steps, FP32.  One bench "step" = one complete
+2000-step simulation from zero fields (1.342e11 cell-updates).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints ONE JSON line (rank 0).  ``value`` is Gcell-updates/s over all ranks
+with inputs resident in HBM; ``e2e`` is the same metric through the public API
+with host buffers (pinned host -> device copies of the initial fields and
+material map, and device -> host copies of all seven result fields, inside the
+timed region).  Under torchrun each rank runs an independent replica (the 2D
+update does not shard on one node here: replicas only), value = total.
+
+``--impl reference`` times the reference's CPU path (the C restatement of
+fd2d/clang/test_3_4.c's loops, float32, OpenMP on all host cores; the
+reference's own C cannot be built on the GPU host) on a bounded sample of the
+same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+NX = NY = 8192
+NPML = 32
+GRADE = 0.333
+RGRID = 1000
+EPSR, SIGMA = 30.0, 0.3
+NS = 2000
+BYTES_PER_CELL_UPDATE = 60  # lossy PML update: 8 float reads + 7 float writes per cell
+METRIC = "Gcell-updates/s & %HBM peak; surrogate vs FDTD spectra/s at ≤1% L2 error"
+UNIT = "Gcell-updates/s"
+WORKLOAD = ("2D TM PML lossy-cylinder benchmark program: 8192x8192, npml=32 grade 0.333, "
+            "cylinder r=1000 eps_r=30 sigma=0.3, hard Gaussian Dz source t0=20 spread=6, 2000 steps, FP32")
+# DRAM bytes per cell per fused pass from the ncu capture of the fused kernel
+# (dram__bytes_read.sum + dram__bytes_write.sum / cells); None until captured
+NCU_TRAFFIC_BYTES_PER_CELL_PASS: float | None = None
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+_CPU_SETUP = {}
+
+
+def _cpu_setup(nx: int, ny: int):
+    """Material map and PML of the benchmark program for the C port (cached)."""
+    import numpy as np
+
+    from oracle import fd2d as O
+    key = (nx, ny)
+    if key not in _CPU_SETUP:
+        dt = 0.01 / 6e8
+        pml = O.pmlparam(nx, ny, NPML, GRADE)
+        naz = np.ones((nx, ny), dtype=np.float32)
+        nbz = np.zeros((nx, ny), dtype=np.float32)
+        for r0 in range(0, nx, 512):  # material map in row bands (float64 formula)
+            a, b = O.dielectric(nx, ny, NPML, RGRID, dt, EPSR, SIGMA, rows=slice(r0, min(nx, r0 + 512)))
+            naz[r0:r0 + a.shape[0]] = a
+            nbz[r0:r0 + b.shape[0]] = b
+        pd = {k: getattr(pml, k) for k in ("fx1", "fx2", "fx3", "fy1", "fy2", "fy3", "gx2", "gx3", "gy2", "gy3")}
+        _CPU_SETUP[key] = (pd, naz, nbz)
+    return _CPU_SETUP[key]
+
+
+def cpu_port_rate(nx: int, ny: int, steps: int, threads: int | None = None) -> dict:
+    """Time the float32 OpenMP C port of the reference loops on this host."""
+    import numpy as np
+
+    from oracle import ccore
+    lib = ccore.lib32()
+    if threads:
+        lib.oracle_set_threads(threads)
+    nth = lib.oracle_threads()
+    pd, naz, nbz = _cpu_setup(nx, ny)
+    f = {k: np.zeros((nx, ny), dtype=np.float32) for k in ("dz", "ez", "iz", "hx", "hy", "ihx", "ihy")}
+    table = np.exp(-0.5 * ((np.arange(1, steps + 2) - 20) / 6.0) ** 2)
+    ccore.fd2d_steps(lib, np.float32, nx, ny, 0, 1, pd, naz, nbz, (1, nx // 2, ny // 2), table, f)  # warm-up
+    t0 = time.perf_counter()
+    ccore.fd2d_steps(lib, np.float32, nx, ny, 1, steps, pd, naz, nbz, (1, nx // 2, ny // 2), table, f)
+    el = time.perf_counter() - t0
+    return {"value": nx * ny * steps / el / 1e9, "seconds": el, "cores": nth,
+            "sample": f"{nx}x{ny} grid, {steps} steps of the same lossy PML update (float32 C port, OpenMP)"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np  # noqa: F401
+    steps_per_sample = int(os.environ.get("FDTD_REF_SAMPLE_STEPS", "4"))
+    for _ in range(args.warmup):
+        cpu_port_rate(NX, NY, 1)
+    vals = []
+    for _ in range(args.steps):
+        r = cpu_port_rate(NX, NY, steps_per_sample)
+        vals.append(r)
+    tot_cells = sum(NX * NY * steps_per_sample for _ in vals)
+    tot_s = sum(v["seconds"] for v in vals)
+    value = tot_cells / tot_s / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / len(vals),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (deterministic benchmark program, no RNG)",
+            "config": {"workload": WORKLOAD, "sample_steps_per_step": steps_per_sample, "grid": [NX, NY]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    import torch.distributed as dist
+
+    from simulation_gb300 import fd2d as G
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sim = G.benchmark_sim(NX, NY, NPML, GRADE, RGRID, EPSR, SIGMA, ns=NS, device=dev,
+                          steps_per_pass=args.spp)
+    spp = args.spp
+    cells = NX * NY
+    passes_per_run = -(-NS // spp)
+    passes_per_run += passes_per_run % 2
+
+    def one_run():
+        sim.reset()
+        sim.step(NS)
+
+    for _ in range(max(args.warmup, 3)):
+        one_run()
+    barrier()
+    clk = Clocks(local)
+    clk.start()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    e0.record(st)
+    for _ in range(args.steps):
+        one_run()
+    e1.record(st)
+    barrier()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    sim.check()
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    total_cells = cells * NS * args.steps * world
+    value = total_cells / (ms / 1e3) / 1e9
+
+    # dominant kernel: time fused passes individually (2 passes of spp steps)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
+    sim.reset()
+    for a, b in ev:
+        a.record(st)
+        sim.step(2 * spp, steps_per_pass=spp)
+        b.record(st)
+    torch.cuda.synchronize()
+    pass_ms = statistics.median(a.elapsed_time(b) for a, b in ev) / 2
+    peak, peak_kind = _peaks()
+    algo_bytes = BYTES_PER_CELL_UPDATE * cells * spp
+    achieved = algo_bytes / (pass_ms / 1e3) / 1e9
+    traffic = None if NCU_TRAFFIC_BYTES_PER_CELL_PASS is None else NCU_TRAFFIC_BYTES_PER_CELL_PASS * cells
+
+    # e2e through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(sim, args, st, world, dev)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS", "8")))
+        cpu["unit"] = UNIT
+        cpu["kind"] = "port"
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (deterministic benchmark program, no RNG)",
+                "config": {"workload": WORKLOAD, "grid": [NX, NY], "time_steps_per_bench_step": NS,
+                           "steps_per_pass": spp, "parallelism": f"replicas x{world}",
+                           "l2": "inputs larger than L2 (3.8 GB of fields per pass)"},
+                "hbm_frac_algorithmic": value * BYTES_PER_CELL_UPDATE / peak,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                             "kernel": f"k_march<K={spp}> (one fused pass = {spp} time steps)",
+                             "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": pass_ms},
+                "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": passes_per_run * args.steps}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_e2e(sim, args, st, world, dev) -> dict:
+    """Same runs through SimTM2D with host (pinned) buffers copied in and out."""
+    import torch
+    keys_in = ("dz", "ez", "iz", "hx", "hy", "ihx", "ihy", "naz", "nbz")
+    keys_out = ("dz", "ez", "iz", "hx", "hy", "ihx", "ihy")
+    host_in = {k: torch.zeros((NX, NY), dtype=torch.float32, pin_memory=True) for k in keys_in}
+    host_in["naz"].copy_(sim.naz.cpu())
+    host_in["nbz"].copy_(sim.nbz.cpu())
+    host_out = {k: torch.empty((NX, NY), dtype=torch.float32, pin_memory=True) for k in keys_out}
+    pml_host = {k: getattr(sim.pml, k).cpu().pin_memory() for k in sim.pml._fields}
+
+    def one():
+        for k in keys_in:
+            getattr(sim, k).copy_(host_in[k], non_blocking=True)
+        for k, v in pml_host.items():
+            getattr(sim.pml, k).copy_(v, non_blocking=True)
+        sim.t = 0
+        sim.step(NS)
+        for k in keys_out:
+            host_out[k].copy_(getattr(sim, k), non_blocking=True)
+
+    one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        one()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    h2d = sum(v.numel() * 4 for v in host_in.values()) + sum(v.numel() * 4 for v in pml_host.values())
+    d2h = sum(v.numel() * 4 for v in host_out.values())
+    return {"value": NX * NY * NS * args.steps * world / (ms / 1e3) / 1e9, "unit": UNIT,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms / args.steps}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--spp", type=int, default=4, help="time steps per fused pass (1..4)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

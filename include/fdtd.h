@@ -1,0 +1,233 @@
+/* fdtd.h -- C-ABI of the GB300 (sm_103a) FDTD library, libfdtd_gb300.so.
+ *
+ * Drop-in replacement for the time-step hot path of dsarvan/simulation:
+ *   (a) the 1D Ex/Hy leapfrog of fd1d (free space, dielectric, lossy, D-form,
+ *       Debye; two-step-back ABC; Gaussian/sinusoidal hard/soft sources;
+ *       running-DFT probes), and
+ *   (b) the 2D TM Dz/Ez/Hx/Hy update of fd2d with its 1D-profile PML
+ *       (gx2/gx3/gy2/gy3, fx1..fx3, fy1..fy3, ihx/ihy accumulators), lossy
+ *       medium (naz/nbz/iz), point sources, TF/SF plane wave and running DFT.
+ *
+ * Conventions (every entry point):
+ *   - returns int: FDTD_OK (0) or a negative FDTD_ERR_* code; nothing throws;
+ *   - argument checks happen on the host BEFORE any launch; a failed check
+ *     launches nothing and leaves every buffer untouched;
+ *   - buffers are caller-owned DEVICE pointers (e.g. torch.Tensor.data_ptr()),
+ *     float32, contiguous; 2D arrays are row-major [nx][ny] with j fastest
+ *     (n = i*ny + j, as in fd2d/clang/fd2d_3_2.c:33);
+ *   - work is enqueued on the given stream (a cudaStream_t; 0 = legacy
+ *     default stream) with no host synchronisation, so calls can be captured
+ *     into a CUDA graph;
+ *   - per-step source values are read from a caller-provided device table
+ *     (table[t-1] is the value at step t) computed on the host in float64, so
+ *     graph replays need no argument changes;
+ *   - calls on one simulation state must be serialised by the caller; any
+ *     host thread may call.
+ *
+ * The reference has no library API: its "interface" is the per-program step
+ * functions (dfield/efield/hfield, exfield/hyfield/dxfield, fourier) that mutate
+ * caller-owned arrays in place.  Each entry point below names the reference
+ * function(s) it replaces, by file:line in dsarvan/simulation.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* every declaration below is exported from the shared library even when it is
+ * built with -fvisibility=hidden */
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+typedef void* fdtd_stream_t; /* a cudaStream_t */
+
+/* ------------------------------------------------------------ status codes */
+#define FDTD_OK 0
+#define FDTD_ERR_NULL (-1)        /* a required pointer is NULL */
+#define FDTD_ERR_SIZE (-2)        /* nx/ny/npml/step counts out of range */
+#define FDTD_ERR_ALIGN (-3)       /* a pointer is not 16-byte aligned where required */
+#define FDTD_ERR_ARG (-4)         /* any other invalid argument */
+#define FDTD_ERR_CUDA (-5)        /* a CUDA call failed (see fdtd_last_cuda_error) */
+#define FDTD_ERR_NONFINITE (-6)   /* the device status word reports Inf/NaN */
+#define FDTD_ERR_TIMEOUT (-7)     /* a bounded device wait ran out */
+#define FDTD_ERR_UNSUPPORTED (-8) /* combination not implemented */
+#define FDTD_ERR_WORKSPACE (-9)   /* workspace missing or too small */
+
+/* device status word bits (an int the caller owns; kernels OR bits in) */
+#define FDTD_STATUS_NONFINITE 1
+#define FDTD_STATUS_TIMEOUT 2
+#define FDTD_STATUS_BOUNDS 4
+
+/* source kinds */
+#define FDTD_SRC_NONE 0
+#define FDTD_SRC_HARD 1 /* field[k] = value   (fd1d/program/fd1d_1_1.py:43, fd2d/python/fd2d_3_1.py:53) */
+#define FDTD_SRC_SOFT 2 /* field[k] += value  (fd1d/program/fd1d_1_3.py:57) */
+
+/* library version, e.g. 100 for 0.1.0 */
+int fdtd_version(void);
+/* human-readable text of an FDTD_ERR_* code */
+const char* fdtd_status_string(int status);
+/* last CUDA error code recorded by an entry point (0 if none) */
+int fdtd_last_cuda_error(void);
+/* decode a device status word read back by the caller into FDTD_OK / FDTD_ERR_* */
+int fdtd_status_to_error(int device_status);
+
+/* ================================================================= 2D TM */
+
+/* pmlayer, fd2d/python/fd2d_3_2.py:47-52 (device pointers, float32).
+ * All ten NULL selects the update without PML or accumulators
+ * (fd2d/python/fd2d_3_1.py:57-72). */
+typedef struct {
+  const float *fx1, *fx2, *fx3; /* [nx] */
+  const float *fy1, *fy2, *fy3; /* [ny] */
+  const float *gx2, *gx3;       /* [nx] */
+  const float *gy2, *gy3;       /* [ny] */
+} fdtd2d_pml;
+
+typedef struct {
+  int kind;           /* FDTD_SRC_* applied to dz[i][j] right after the D update */
+  int i, j;
+  const float* table; /* device, table[t-1] = value at step t */
+  int table_len;
+} fdtd2d_source;
+
+typedef struct {
+  int nx, ny;
+  fdtd2d_pml pml;
+  const float* naz; /* [nx][ny] 1/(eps_r + sigma*dt/eps0), fd2d/python/fd2d_3_4.py:192 */
+  const float* nbz; /* [nx][ny] sigma*dt/eps0, or NULL for the lossless E update */
+  fdtd2d_source src;
+  /* TF/SF plane-wave source of fd2d/python/fd2d_3_4.py:103-170 (0 = off):
+   * incident line ezi/hxi along j, boundary at npml-1 .. n-npml. */
+  int tfsf_npml;
+  const float* tfsf_table; /* device, ezi[3] = tfsf_table[t-1] (gaussian(t,20,8) in the reference) */
+  int tfsf_table_len;
+  /* running DFT of Ez at every cell, fd2d/python/fd2d_3_4.py:90-99 (nf = 0: off) */
+  int nf;
+  const float* dft_cos; /* device [table_len][nf]: cos(2*pi*f*dt*t) at row t-1 */
+  const float* dft_sin; /* device [table_len][nf] */
+  int dft_table_len;
+} fdtd2d_params;
+
+typedef struct {
+  float *dz, *ez, *iz, *hx, *hy, *ihx, *ihy; /* [nx][ny]; iz NULL if lossless; ihx/ihy NULL without PML */
+  float *ezi, *hxi, *bc;                     /* TF/SF incident line [ny] and its ABC state [4] */
+  float *r_pt, *i_pt;                        /* DFT [nf][nx][ny] */
+  float *r_in, *i_in;                        /* DFT of ezi[6], [nf] */
+  int* status;                               /* device status word, may be NULL */
+} fdtd2d_state;
+
+/* dfield: D update + point source (+ ezi[3] for TF/SF) for step t.
+ * Replaces dfield of fd2d/python/fd2d_3_2.py:62-69, fd2d/python/fd2d_3_4.py:113-119,
+ * fd2d/cuda/fd2d_3_2.cu:34-49. */
+int fdtd2d_dfield(int t, const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+/* efield: Ez (and iz) from Dz. Replaces efield of fd2d/python/fd2d_3_2.py:72-77 and
+ * fd2d/python/fd2d_3_4.py:131-136, fd2d/cuda/fd2d_3_4.cu:99-109. */
+int fdtd2d_efield(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+/* hfield: Hx/Hy (+ ihx/ihy). Replaces hfield of fd2d/python/fd2d_3_2.py:80-88,
+ * fd2d/python/fd2d_3_1.py:66-72, fd2d/cuda/fd2d_3_2.cu:63-76. */
+int fdtd2d_hfield(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+/* TF/SF and DFT pieces at the reference's granularity
+ * (fd2d/python/fd2d_3_4.py:103-110, :123-127, :140-143, :158-170, :90-99). */
+int fdtd2d_ezinct(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+int fdtd2d_inctdz(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+int fdtd2d_hxinct(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+int fdtd2d_incth(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+int fdtd2d_fourier(int t, const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
+
+/* Bytes of device workspace fdtd2d_step_n needs for these params (0 if none). */
+size_t fdtd2d_workspace_size(const fdtd2d_params* p, int steps_per_pass);
+
+/* fdtd2d_step_n: the program's time loop for t = t0+1 .. t0+nsteps, in the
+ * reference's step order (fd2d/python/fd2d_3_4.py:268-277).  The core
+ * D->source->E->H update is fused into one streaming kernel that keeps
+ * `steps_per_pass` (1..4; 0 = library default) time steps in registers per
+ * pass over HBM; `workspace` (fdtd2d_workspace_size bytes, 256-byte aligned)
+ * holds the ping-pong copy of the evolving fields.  Results land in the
+ * caller's arrays, bitwise equal to calling dfield/efield/hfield per step.
+ * With TF/SF or DFT enabled the per-function kernels run instead.
+ * Replaces the `for t in 1..ns` loops of fd2d/python/fd2d_3_2.py:139-142 and
+ * fd2d/cuda/fd2d_3_4.cu:327-336. */
+int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass,
+                  void* workspace, size_t workspace_bytes, fdtd_stream_t stream);
+
+/* Tuning knob of the fused kernel (used by the bench/autotuner): columns per
+ * lane (2 or 4) and rows per warp segment (0 = automatic, one wave of warps).
+ * No reference counterpart. */
+int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows);
+
+/* Lossy-cylinder material map on the device, float64 arithmetic in the order of
+ * dielectric() in fd2d/python/fd2d_3_4.py:174-194 (true division m/3):
+ * writes naz, nbz [nx][ny]. */
+int fdtd2d_dielectric_cylinder(int nx, int ny, int npml, double rgrid, double dt, double epsr,
+                               double sigma, float* naz, float* nbz, fdtd_stream_t stream);
+
+/* Sets *status_out |= FDTD_STATUS_NONFINITE if any of the n floats is Inf/NaN. */
+int fdtd_check_finite(const float* x, size_t n, int* status, fdtd_stream_t stream);
+
+/* ================================================================= 1D */
+
+#define FDTD1D_FORM_CB 0    /* ex += cb*(hy[i-1]-hy[i])            fd1d/program/fd1d_1_3.py:55 */
+#define FDTD1D_FORM_CACB 1  /* ex = ca*ex + cb*(hy[i-1]-hy[i])     fd1d/program/fd1d_1_5.py:65 */
+#define FDTD1D_FORM_DFORM 2 /* dx/ix with nax/nbx                   fd1d/program/fd1d_2_2.py:74-84 */
+#define FDTD1D_FORM_DEBYE 3 /* D-form + Debye sx with ncx/ndx       fd1d/program/fd1d_2_3.py:82-86 */
+
+#define FDTD1D_MAX_PROBES 8
+
+typedef struct {
+  int nx;
+  int form;                                      /* FDTD1D_FORM_* */
+  const float *ca, *cb;                          /* [nx]: CB uses cb; CACB uses ca, cb */
+  const float *nax, *nbx, *ncx, *ndx;            /* [nx]: DFORM uses nax, nbx; DEBYE all four */
+  int src_kind;                                  /* FDTD_SRC_*; into ex (CB/CACB) or dx (D forms) */
+  int src_k;
+  const float* src_table;                        /* device, table[t-1] */
+  int src_table_len;
+  int abc;                                       /* 1: two-step-back ABC, fd1d/program/fd1d_1_2.py:47-48 */
+  int nf;                                        /* running DFT frequencies (0 = off) */
+  const float* dft_cos;                          /* device [table_len][nf] */
+  const float* dft_sin;
+  int dft_table_len;
+  int nprobe;                                    /* probe cells (<= FDTD1D_MAX_PROBES) */
+  int probe_k[FDTD1D_MAX_PROBES];
+  int full_dft;                                  /* 1: accumulate every cell into r_pt/i_pt */
+} fdtd1d_params;
+
+typedef struct {
+  float *ex, *hy;      /* [nx] */
+  float *dx, *ix, *sx; /* [nx] D forms (sx: Debye) */
+  float* bc;           /* [4] ABC state */
+  float *r_pt, *i_pt;  /* [nf][nx] when full_dft */
+  float *r_pr, *i_pr;  /* [nprobe][nf] probe DFT accumulators */
+  int* status;
+} fdtd1d_state;
+
+/* exfield (+ source), fd1d/clang/fd1d_1_3.c:17-23 and fd1d/program/fd1d_1_5.py:65-67;
+ * for the D forms: dxfield + exfield, fd1d/program/fd1d_2_2.py:74-84. */
+int fdtd1d_efield(int t, const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t stream);
+/* hyfield: ABC then Hy, fd1d/program/fd1d_2_2.py:87-92, fd1d/clang/fd1d_1_3.c:26-33. */
+int fdtd1d_hfield(const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t stream);
+/* fourier, fd1d/program/fd1d_2_2.py:65-71 (probes and optionally every cell). */
+int fdtd1d_fourier(int t, const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t stream);
+/* fdtd1d_step_n: the program's time loop, t = t0+1 .. t0+nsteps, in one launch
+ * (one thread-block cluster holds the whole line in registers; warp shuffles
+ * and distributed shared memory carry the halos).  nx up to 131072.
+ * Replaces fd1d/program/fd1d_1_3.py:53-62, fd1d/program/fd1d_2_2.py:138-142,
+ * fd1d/cuda/fd1d_1_3.cu:78-85. */
+int fdtd1d_step_n(const fdtd1d_params* p, fdtd1d_state* s, int t0, int nsteps, fdtd_stream_t stream);
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDTD_GB300_H */

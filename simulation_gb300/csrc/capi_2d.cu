@@ -1,0 +1,244 @@
+// C-ABI entry points of the 2D TM path: argument checks, then launches.
+#include <vector>
+
+#include "fd2d_internal.cuh"
+
+namespace {
+
+using namespace fdtd;
+
+inline bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+int check_params(const fdtd2d_params* p, const fdtd2d_state* s, int t_last, bool need_e, bool need_h) {
+  if (!p || !s) return FDTD_ERR_NULL;
+  if (p->nx < 3 || p->ny < 3) return FDTD_ERR_SIZE;
+  if ((long long)p->nx * p->ny > (1LL << 34)) return FDTD_ERR_SIZE;
+  if (!s->dz || !s->ez || !s->hx || !s->hy || !p->naz) return FDTD_ERR_NULL;
+  if (p->nbz && !s->iz) return FDTD_ERR_NULL;
+  const fdtd2d_pml& m = p->pml;
+  const int npml_ptrs = (m.fx1 != nullptr) + (m.fx2 != nullptr) + (m.fx3 != nullptr) + (m.fy1 != nullptr) +
+                        (m.fy2 != nullptr) + (m.fy3 != nullptr) + (m.gx2 != nullptr) + (m.gx3 != nullptr) +
+                        (m.gy2 != nullptr) + (m.gy3 != nullptr);
+  if (npml_ptrs != 0 && npml_ptrs != 10) return FDTD_ERR_NULL;
+  if (npml_ptrs == 10 && need_h && (!s->ihx || !s->ihy)) return FDTD_ERR_NULL;
+  if (p->src.kind < FDTD_SRC_NONE || p->src.kind > FDTD_SRC_SOFT) return FDTD_ERR_ARG;
+  if (p->src.kind != FDTD_SRC_NONE) {
+    if (p->src.i < 0 || p->src.i >= p->nx || p->src.j < 0 || p->src.j >= p->ny) return FDTD_ERR_ARG;
+    if (!p->src.table) return FDTD_ERR_NULL;
+    if (t_last > p->src.table_len) return FDTD_ERR_SIZE;
+  }
+  if (p->tfsf_npml < 0) return FDTD_ERR_SIZE;
+  if (p->tfsf_npml > 0) {
+    if (p->tfsf_npml < 2 || 2 * p->tfsf_npml >= p->nx || 2 * p->tfsf_npml >= p->ny || p->ny < 7)
+      return FDTD_ERR_SIZE;
+    if (!s->ezi || !s->hxi || !s->bc || !p->tfsf_table) return FDTD_ERR_NULL;
+    if (t_last > p->tfsf_table_len) return FDTD_ERR_SIZE;
+  }
+  if (p->nf < 0) return FDTD_ERR_SIZE;
+  if (p->nf > 0) {
+    if (p->nf > 1024) return FDTD_ERR_SIZE;
+    if (!p->dft_cos || !p->dft_sin || !s->r_pt || !s->i_pt) return FDTD_ERR_NULL;
+    if (p->tfsf_npml > 0 && (!s->r_in || !s->i_in)) return FDTD_ERR_NULL;
+    if (t_last > p->dft_table_len) return FDTD_ERR_SIZE;
+  }
+  (void)need_e;
+  return FDTD_OK;
+}
+
+bool fused_ok(const fdtd2d_params* p, const fdtd2d_state* s) {
+  if (p->tfsf_npml > 0 || p->nf > 0) return false;
+  if (p->ny % 4 != 0) return false;
+  const void* ptrs[] = {s->dz, s->ez, s->hx, s->hy, p->naz};
+  for (const void* q : ptrs)
+    if (!aligned16(q)) return false;
+  if (p->nbz && (!aligned16(p->nbz) || !aligned16(s->iz))) return false;
+  if (has_pml(*p) && (!aligned16(s->ihx) || !aligned16(s->ihy))) return false;
+  return true;
+}
+
+size_t slot_bytes(const fdtd2d_params* p) {
+  const size_t b = (size_t)p->nx * p->ny * sizeof(float);
+  return (b + 255) & ~(size_t)255;
+}
+
+int nslots(const fdtd2d_params* p) { return 3 + (p->nbz ? 1 : 0) + (has_pml(*p) ? 2 : 0); }
+
+// one time step with the per-function kernels, in the reference's order
+// (fd2d/python/fd2d_3_4.py:268-277)
+int step_per_function(int t, const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st) {
+  int rc;
+  const bool tfsf = p.tfsf_npml > 0;
+  if (tfsf && (rc = launch_ezinct(p, s, st))) return rc;
+  if ((rc = launch_dfield(t, p, s, st))) return rc;
+  if (tfsf && (rc = launch_inctdz(p, s, st))) return rc;
+  if ((rc = launch_efield(p, s, st))) return rc;
+  if (p.nf > 0 && (rc = launch_fourier(t, p, s, st))) return rc;
+  if (tfsf && (rc = launch_hxinct(p, s, st))) return rc;
+  if ((rc = launch_hfield(p, s, st))) return rc;
+  if (tfsf && (rc = launch_incth(p, s, st))) return rc;
+  return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fdtd2d_dfield(int t, const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, t, false, false);
+  if (rc) return rc;
+  if (t < 1) return FDTD_ERR_ARG;
+  return launch_dfield(t, *p, *s, (cudaStream_t)stream);
+}
+
+int fdtd2d_efield(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, 0, true, false);
+  if (rc) return rc;
+  return launch_efield(*p, *s, (cudaStream_t)stream);
+}
+
+int fdtd2d_hfield(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, 0, false, true);
+  if (rc) return rc;
+  return launch_hfield(*p, *s, (cudaStream_t)stream);
+}
+
+int fdtd2d_ezinct(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, 0, false, false);
+  if (rc) return rc;
+  if (p->tfsf_npml <= 0) return FDTD_ERR_ARG;
+  return launch_ezinct(*p, *s, (cudaStream_t)stream);
+}
+
+int fdtd2d_inctdz(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, 0, false, false);
+  if (rc) return rc;
+  if (p->tfsf_npml <= 0) return FDTD_ERR_ARG;
+  return launch_inctdz(*p, *s, (cudaStream_t)stream);
+}
+
+int fdtd2d_hxinct(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, 0, false, false);
+  if (rc) return rc;
+  if (p->tfsf_npml <= 0) return FDTD_ERR_ARG;
+  return launch_hxinct(*p, *s, (cudaStream_t)stream);
+}
+
+int fdtd2d_incth(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, 0, false, false);
+  if (rc) return rc;
+  if (p->tfsf_npml <= 0) return FDTD_ERR_ARG;
+  return launch_incth(*p, *s, (cudaStream_t)stream);
+}
+
+int fdtd2d_fourier(int t, const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream) {
+  int rc = check_params(p, s, t, false, false);
+  if (rc) return rc;
+  if (t < 1 || p->nf <= 0) return FDTD_ERR_ARG;
+  return launch_fourier(t, *p, *s, (cudaStream_t)stream);
+}
+
+size_t fdtd2d_workspace_size(const fdtd2d_params* p, int steps_per_pass) {
+  (void)steps_per_pass;
+  if (!p || p->nx < 3 || p->ny < 3) return 0;
+  if (p->tfsf_npml > 0 || p->nf > 0 || p->ny % 4 != 0) return 0;
+  return slot_bytes(p) * nslots(p);
+}
+
+int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass, void* workspace,
+                  size_t workspace_bytes, fdtd_stream_t stream) {
+  if (t0 < 0 || nsteps < 0) return FDTD_ERR_ARG;
+  int rc = check_params(p, s, t0 + nsteps, true, true);
+  if (rc) return rc;
+  if (steps_per_pass < 0 || steps_per_pass > march_max_steps_per_pass()) return FDTD_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (nsteps == 0) return FDTD_OK;
+
+  if (!fused_ok(p, s) || nsteps == 1) {
+    for (int t = t0 + 1; t <= t0 + nsteps; ++t)
+      if ((rc = step_per_function(t, *p, *s, st))) return rc;
+    if (s->status) launch_check_finite(s->ez, (size_t)p->nx * p->ny, s->status, st);
+    return fdtd_host::check_launch();
+  }
+
+  const size_t need = slot_bytes(p) * nslots(p);
+  if (!workspace || workspace_bytes < need) return FDTD_ERR_WORKSPACE;
+  if (((uintptr_t)workspace & 255u) != 0) return FDTD_ERR_ALIGN;
+
+  // pass schedule with an even number of passes, so the last pass writes the
+  // caller's arrays (split one pass if needed)
+  const int K = steps_per_pass == 0 ? march_max_steps_per_pass() : steps_per_pass;
+  std::vector<int> sched;
+  for (int rem = nsteps; rem > 0;) {
+    const int k = rem < K ? rem : K;
+    sched.push_back(k);
+    rem -= k;
+  }
+  bool copy_back = false;
+  if (sched.size() % 2 == 1) {
+    size_t idx = sched.size();
+    for (size_t i = 0; i < sched.size(); ++i)
+      if (sched[i] >= 2) {
+        idx = i;
+        break;
+      }
+    if (idx < sched.size()) {
+      const int k = sched[idx];
+      sched[idx] = k / 2;
+      sched.insert(sched.begin() + idx + 1, k - k / 2);
+    } else {
+      copy_back = true;
+    }
+  }
+
+  FieldSet user{s->dz, s->iz, s->hx, s->hy, s->ihx, s->ihy};
+  FieldSet ws{};
+  {
+    char* base = (char*)workspace;
+    const size_t sb = slot_bytes(p);
+    int k = 0;
+    ws.dz = (float*)(base + sb * k++);
+    ws.hx = (float*)(base + sb * k++);
+    ws.hy = (float*)(base + sb * k++);
+    if (p->nbz) ws.iz = (float*)(base + sb * k++);
+    if (has_pml(*p)) {
+      ws.ihx = (float*)(base + sb * k++);
+      ws.ihy = (float*)(base + sb * k++);
+    }
+  }
+  int t = t0;
+  for (size_t i = 0; i < sched.size(); ++i) {
+    const FieldSet& in = (i % 2 == 0) ? user : ws;
+    const FieldSet& out = (i % 2 == 0) ? ws : user;
+    if ((rc = launch_march(*p, in, out, s->ez, t, sched[i], s->status, st))) return rc;
+    t += sched[i];
+  }
+  if (copy_back) {
+    const size_t b = (size_t)p->nx * p->ny * sizeof(float);
+    float* pairs[6][2] = {{user.dz, ws.dz}, {user.hx, ws.hx}, {user.hy, ws.hy},
+                          {user.iz, ws.iz}, {user.ihx, ws.ihx}, {user.ihy, ws.ihy}};
+    for (auto& pr : pairs)
+      if (pr[0] && pr[1]) {
+        const cudaError_t e = cudaMemcpyAsync(pr[0], pr[1], b, cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) {
+          fdtd_host::note_cuda_error(e);
+          return FDTD_ERR_CUDA;
+        }
+      }
+  }
+  return FDTD_OK;
+}
+
+int fdtd2d_dielectric_cylinder(int nx, int ny, int npml, double rgrid, double dt, double epsr, double sigma,
+                               float* naz, float* nbz, fdtd_stream_t stream) {
+  if (!naz || !nbz) return FDTD_ERR_NULL;
+  if (nx < 3 || ny < 3 || npml < 0 || 2 * npml > nx || 2 * npml > ny) return FDTD_ERR_SIZE;
+  if (!(dt > 0) || !(epsr > 0) || sigma < 0) return FDTD_ERR_ARG;
+  return launch_dielectric(nx, ny, npml, rgrid, dt, epsr, sigma, naz, nbz, (cudaStream_t)stream);
+}
+
+int fdtd_check_finite(const float* x, size_t n, int* status, fdtd_stream_t stream) {
+  if (!x || !status) return FDTD_ERR_NULL;
+  return launch_check_finite(x, n, status, (cudaStream_t)stream);
+}
+
+}  // extern "C"

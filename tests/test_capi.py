@@ -1,0 +1,77 @@
+"""The C-ABI library loads, exports every symbol include/fdtd.h declares, and
+rejects bad arguments on the host before any launch (no GPU needed)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+from tests.conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from simulation_gb300 import build
+    build.build()
+    from simulation_gb300 import _lib
+    return _lib.lib()
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "fdtd.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\**\s+\**(fdtd[a-z0-9_]*)\s*\(", src, flags=re.M)))
+
+
+def test_exports_every_declared_symbol(lib):
+    names = _declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared in include/fdtd.h but not exported"
+    from simulation_gb300 import _lib
+    assert set(_lib.declared_symbols()) <= set(names) | {"fdtd_version"}
+
+
+def test_status_strings(lib):
+    assert lib.fdtd_version() >= 100
+    assert lib.fdtd_status_string(0) == b"ok"
+    assert lib.fdtd_status_to_error(1) == -6
+    assert lib.fdtd_status_to_error(2) == -7
+    assert lib.fdtd_status_to_error(0) == 0
+
+
+def test_argument_checks_without_gpu(lib):
+    """Every check runs on the host before any CUDA call, so bad arguments are
+    reported even on a machine with no GPU."""
+    from simulation_gb300 import _lib
+    p = _lib.Params2D()
+    s = _lib.State2D()
+    assert lib.fdtd2d_step_n(None, None, 0, 1, 0, None, 0, None) == -1
+    p.nx, p.ny = 2, 64
+    assert lib.fdtd2d_step_n(C.byref(p), C.byref(s), 0, 1, 0, None, 0, None) == -2
+    p.nx, p.ny = 64, 64
+    assert lib.fdtd2d_step_n(C.byref(p), C.byref(s), 0, 1, 0, None, 0, None) == -1  # NULL fields
+    fake = 0x10000  # never dereferenced: the calls below fail their checks first
+    for k in ("dz", "ez", "hx", "hy"):
+        setattr(s, k, fake)
+    p.naz = fake
+    p.pml.fx1 = fake  # 1 of 10 PML pointers
+    assert lib.fdtd2d_step_n(C.byref(p), C.byref(s), 0, 1, 0, None, 0, None) == -1
+    p.pml.fx1 = None
+    p.src.kind, p.src.i, p.src.j = 1, 70, 3
+    assert lib.fdtd2d_step_n(C.byref(p), C.byref(s), 0, 1, 0, None, 0, None) == -4
+    p.src.i = 3
+    p.src.table, p.src.table_len = fake, 5
+    assert lib.fdtd2d_step_n(C.byref(p), C.byref(s), 0, 10, 0, None, 0, None) == -2  # table too short
+    assert lib.fdtd2d_step_n(C.byref(p), C.byref(s), 0, 2, 9, None, 0, None) == -4  # steps per pass
+    assert lib.fdtd2d_step_n(C.byref(p), C.byref(s), -1, 2, 0, None, 0, None) == -4
+    q = _lib.Params1D()
+    t = _lib.State1D()
+    q.nx = 3
+    assert lib.fdtd1d_step_n(C.byref(q), C.byref(t), 0, 1, None) == -2
+    q.nx, q.form = 64, 7
+    t.ex = t.hy = fake
+    assert lib.fdtd1d_step_n(C.byref(q), C.byref(t), 0, 1, None) == -4
+    q.form = 0
+    assert lib.fdtd1d_step_n(C.byref(q), C.byref(t), 0, 1, None) == -1  # cb missing
+    assert lib.fdtd2d_dielectric_cylinder(64, 64, 40, 10.0, 1e-11, 30.0, 0.3, fake, fake, None) == -2
