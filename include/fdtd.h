@@ -179,6 +179,7 @@ int fdtd_check_finite(const float* x, size_t n, int* status, fdtd_stream_t strea
 #define FDTD1D_FORM_DEBYE 3 /* D-form + Debye sx with ncx/ndx       fd1d/program/fd1d_2_3.py:82-86 */
 
 #define FDTD1D_MAX_PROBES 8
+#define FDTD1D_MAX_FUSED_NX 65536
 
 typedef struct {
   int nx;
@@ -217,7 +218,9 @@ int fdtd1d_hfield(const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t stream)
 int fdtd1d_fourier(int t, const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t stream);
 /* fdtd1d_step_n: the program's time loop, t = t0+1 .. t0+nsteps, in one launch
  * (one thread-block cluster holds the whole line in registers; warp shuffles
- * and distributed shared memory carry the halos).  nx up to 131072.
+ * and distributed shared memory carry the halos).  nx <= FDTD1D_MAX_FUSED_NX
+ * (8 blocks x 512 threads x 16 cells); longer lines use the per-function
+ * entry points above.
  * Replaces fd1d/program/fd1d_1_3.py:53-62, fd1d/program/fd1d_2_2.py:138-142,
  * fd1d/cuda/fd1d_1_3.cu:78-85. */
 int fdtd1d_step_n(const fdtd1d_params* p, fdtd1d_state* s, int t0, int nsteps, fdtd_stream_t stream);

@@ -129,7 +129,7 @@ struct Run1DArgs {
 
 constexpr int RUN1D_MAX_THREADS = 1024;
 // block size limit per cells-per-thread, so the register budget grows with CPT
-__host__ __device__ constexpr int run1d_max_threads(int cpt) { return cpt <= 4 ? 1024 : (cpt == 8 ? 512 : 256); }
+__host__ __device__ constexpr int run1d_max_threads(int cpt) { return cpt <= 8 ? 1024 : 512; }
 
 template <int FORM, int CPT, bool CLUSTER>
 __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1DArgs a) {
@@ -555,7 +555,7 @@ int fdtd1d_step_n(const fdtd1d_params* p, fdtd1d_state* s, int t0, int nsteps, f
   int rc = check1d(p, s, t0 + nsteps);
   if (rc) return rc;
   if (nsteps == 0) return FDTD_OK;
-  if (p->nx > 131072) return FDTD_ERR_SIZE;
+  if (p->nx > FDTD1D_MAX_FUSED_NX) return FDTD_ERR_SIZE;
   return fdtd::launch_fd1d_run(*p, *s, t0, nsteps, (cudaStream_t)stream);
 }
 

@@ -136,9 +136,15 @@ class Sim1D:
         if t_last > self._ns:
             self._tables(max(t_last, 2 * self._ns))
 
+    MAX_FUSED_NX = 65536  # FDTD1D_MAX_FUSED_NX
+
     def step(self, n: int = 1) -> None:
-        """Advance n steps in one fused launch (one thread-block cluster)."""
+        """Advance n steps: one fused launch (one thread-block cluster) when the
+        line fits on-chip, else one launch per reference function per step."""
         if n <= 0:
+            return
+        if self.nx > self.MAX_FUSED_NX:
+            self.step_per_function(n)
             return
         self._ensure(self.t + n)
         call("fdtd1d_step_n", self._p, self._s, self.t, n, _lib.stream_ptr())
