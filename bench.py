@@ -323,9 +323,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--spp", type=int, default=4, help="time steps per fused pass (1..4)")
+    ap.add_argument("--grid", type=int, default=8192, help="grid edge (profiling runs use a smaller case)")
+    ap.add_argument("--ns", type=int, default=2000, help="time steps per bench step")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    global NX, NY, NS
+    NX = NY = args.grid
+    NS = args.ns
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -158,7 +158,8 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
                   void* workspace, size_t workspace_bytes, fdtd_stream_t stream);
 
 /* Tuning knob of the fused kernel (used by the bench/autotuner): columns per
- * lane (2 or 4) and rows per warp segment (0 = automatic, one wave of warps).
+ * lane (2 or 4; 0 = automatic) and rows per warp segment (0 = automatic, one
+ * wave of warps).
  * No reference counterpart. */
 int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows);
 
@@ -224,6 +225,53 @@ int fdtd1d_fourier(int t, const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t
  * Replaces fd1d/program/fd1d_1_3.py:53-62, fd1d/program/fd1d_2_2.py:138-142,
  * fd1d/cuda/fd1d_1_3.cu:78-85. */
 int fdtd1d_step_n(const fdtd1d_params* p, fdtd1d_state* s, int t0, int nsteps, fdtd_stream_t stream);
+
+/* ================================================================= batched 1D
+ * Thousands of independent lossy 1D runs (ca/cb update of
+ * fd1d/program/fd1d_1_5.py:63-72 with a soft source and the two-step-back ABC)
+ * of uneven length, each with a piecewise-constant layer table, in one
+ * persistent launch; the running DFT of fd1d/program/fd1d_2_2.py:65-71 is
+ * accumulated at an entry and an exit probe.  No reference counterpart: the
+ * reference runs one program at a time. */
+typedef struct {
+  int nruns;
+  const int* ke;          /* device [nruns]: cells of each run (>= 4) */
+  const int* layer_off;   /* device [nruns+1]: run r's layers are layer_off[r] .. layer_off[r+1]-1 */
+  int nlayers;
+  const int* layer_start; /* device [nlayers]: first cell of the layer */
+  const int* layer_end;   /* device [nlayers]: one past its last cell */
+  const float* layer_ca;  /* device [nlayers]: ca, cb of the layer (cells outside layers: ca=1, cb=0.5) */
+  const float* layer_cb;
+  const int* probe_in;    /* device [nruns]: entry probe cell */
+  const int* probe_out;   /* device [nruns]: exit probe cell */
+  int src_k;              /* soft source cell (all runs), >= 1 */
+  const float* src_table; /* device [nsteps] */
+  int nsteps;
+  int nf;                 /* 1..64 */
+  const float* dft_cos;   /* device [nsteps][nf] */
+  const float* dft_sin;
+} fdtd1d_batch_params;
+
+typedef struct {
+  float* spec;      /* device [nruns][4][nf]: re/im at the entry probe, re/im at the exit probe */
+  int* done;        /* device [nruns] or NULL: 1 when the run completed */
+  int* status;      /* device status word or NULL */
+  unsigned* queue;  /* device work counter (one unsigned), reset by the call */
+} fdtd1d_batch_out;
+
+/* Host-side planner (no device work): team size per run = ceil(ke/cells_per_thread)
+ * threads rounded to whole warps, teams packed first-fit-decreasing into blocks
+ * of block_threads.  Writes the plan (int32) to `plan` (NULL: only *plan_len). */
+int fdtd1d_batch_plan(const int* ke_host, int nruns, int cells_per_thread, int block_threads, int* plan,
+                      size_t plan_ints, int* plan_len);
+/* Runs the planned batch: plan_device is the plan copied to the device;
+ * cells_per_thread and block_threads must match the plan: cells_per_thread 8 or
+ * 16 with blocks of up to 1024 threads, 24, 32 or 40 with up to 512;
+ * ctas_per_sm 0 = as many as fit; max_cycles > 0 bounds each block's time for
+ * taking new work (FDTD_STATUS_TIMEOUT if work was left). */
+int fdtd1d_batch_run(const fdtd1d_batch_params* p, fdtd1d_batch_out* o, const int* plan_device, int plan_len,
+                     int nbundles, int cells_per_thread, int block_threads, int ctas_per_sm, long long max_cycles,
+                     fdtd_stream_t stream);
 
 #if defined(__GNUC__)
 #pragma GCC visibility pop

@@ -75,6 +75,17 @@ class State1D(C.Structure):
         ("status", P)]
 
 
+class BatchParams1D(C.Structure):
+    _fields_ = [("nruns", C.c_int), ("ke", P), ("layer_off", P), ("nlayers", C.c_int), ("layer_start", P),
+                ("layer_end", P), ("layer_ca", F), ("layer_cb", F), ("probe_in", P), ("probe_out", P),
+                ("src_k", C.c_int), ("src_table", F), ("nsteps", C.c_int), ("nf", C.c_int), ("dft_cos", F),
+                ("dft_sin", F)]
+
+
+class BatchOut1D(C.Structure):
+    _fields_ = [("spec", F), ("done", P), ("status", P), ("queue", P)]
+
+
 _SIGS = {
     "fdtd_version": ([], C.c_int),
     "fdtd_status_string": ([C.c_int], C.c_char_p),
@@ -99,6 +110,9 @@ _SIGS = {
     "fdtd1d_hfield": ([C.POINTER(Params1D), C.POINTER(State1D), P], C.c_int),
     "fdtd1d_fourier": ([C.c_int, C.POINTER(Params1D), C.POINTER(State1D), P], C.c_int),
     "fdtd1d_step_n": ([C.POINTER(Params1D), C.POINTER(State1D), C.c_int, C.c_int, P], C.c_int),
+    "fdtd1d_batch_plan": ([P, C.c_int, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_int)], C.c_int),
+    "fdtd1d_batch_run": ([C.POINTER(BatchParams1D), C.POINTER(BatchOut1D), P, C.c_int, C.c_int, C.c_int, C.c_int,
+                          C.c_int, C.c_longlong, P], C.c_int),
 }
 
 _LIB = None

@@ -1,0 +1,295 @@
+"""Batched uneven 1D slab runs on the GPU, with fused DFT probes and an autotuner.
+
+Each run is the lossy ca/cb 1D program of fd1d/program/fd1d_1_5.py (E update,
+soft Gaussian source, two-step-back ABC, H update) on its own grid length with
+a stack of dielectric layers; the running DFT of fd1d/program/fd1d_2_2.py:65-71
+is accumulated at an entry probe (between source and stack, like the
+reference's input probe ex[10]) and an exit probe (behind the stack), and the
+transmission is T(f) = DFT_exit/DFT_entry with the reference's amplitude/phase
+convention (fd1d/program/fd1d_2_2.py:145-146).
+
+All runs go into one persistent launch (``libfdtd_gb300.so``,
+``fdtd1d_batch_run``); a C++ planner in the library sizes one team of warps per
+run and packs teams into thread blocks; ``autotune`` picks cells-per-thread,
+block size and blocks-per-SM by timing candidates on a short prefix of the
+time loop.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .sources import dft_tables, to_device, wave_values
+
+EPS0 = 8.854e-12  # fd1d/program/fd1d_1_5.py:40
+DS = 0.01
+DT = DS / 6e8
+
+# (cells per thread, largest block) pairs the library is compiled for
+VARIANTS = ((8, 1024), (16, 1024), (24, 512), (32, 512), (40, 512))
+
+
+def layer_coeffs(epsr, sigma, dt: float = DT):
+    """(ca, cb) of a lossy layer, fd1d/program/fd1d_1_5.py:37-44 (float64)."""
+    epsr = np.asarray(epsr, dtype=np.float64)
+    sigma = np.asarray(sigma, dtype=np.float64)
+    epsf = dt * sigma / (2 * EPS0 * epsr)
+    return (1 - epsf) / (1 + epsf), 0.5 / (epsr * (1 + epsf))
+
+
+@dataclass
+class SlabBatch:
+    """Layered slab runs: ``ke[r]`` cells; run r's layers are rows
+    ``layer_off[r]:layer_off[r+1]`` of (start, end, epsr, sigma)."""
+    ke: np.ndarray
+    layer_off: np.ndarray
+    layer_start: np.ndarray
+    layer_end: np.ndarray
+    epsr: np.ndarray
+    sigma: np.ndarray
+    probe_in: np.ndarray
+    probe_out: np.ndarray
+    src_k: int = 20
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def nruns(self) -> int:
+        return int(self.ke.size)
+
+    def subset(self, idx) -> "SlabBatch":
+        idx = np.asarray(idx)
+        offs = [0]
+        ls, le, er, sg = [], [], [], []
+        for r in idx:
+            a, b = self.layer_off[r], self.layer_off[r + 1]
+            ls += list(self.layer_start[a:b])
+            le += list(self.layer_end[a:b])
+            er += list(self.epsr[a:b])
+            sg += list(self.sigma[a:b])
+            offs.append(len(ls))
+        return SlabBatch(self.ke[idx].copy(), np.array(offs), np.array(ls, dtype=np.int64),
+                         np.array(le, dtype=np.int64), np.array(er), np.array(sg), self.probe_in[idx].copy(),
+                         self.probe_out[idx].copy(), self.src_k, dict(self.meta))
+
+    def coefficients(self, r: int):
+        """Full per-cell (ca, cb) float64 arrays of run r (for the oracle)."""
+        ke = int(self.ke[r])
+        ca = np.ones(ke)
+        cb = np.full(ke, 0.5)
+        a, b = self.layer_off[r], self.layer_off[r + 1]
+        lca, lcb = layer_coeffs(self.epsr[a:b], self.sigma[a:b])
+        for k in range(b - a):
+            s, e = int(self.layer_start[a + k]), int(self.layer_end[a + k])
+            ca[s:e] = lca[k]
+            cb[s:e] = lcb[k]
+        return ca, cb
+
+
+def slab_batch(nruns: int = 4096, seed: int = 0, ke_range=(500, 20000), layers=(1, 8), thick=(20, 400),
+               epsr=(1.0, 9.0), sigma=(0.0, 0.05), src_k: int = 20, stack_start: int = 40,
+               probe_gap: int = 10) -> SlabBatch:
+    """Seeded synthetic batch of the batched-slab workload.
+
+    ke ~ U[500, 20000]; 1..8 layers of thickness U[20, 400], eps_r ~ U[1, 9],
+    sigma ~ U[0, 0.05] S/m, stacked from cell ``stack_start``; the source sits
+    at ``src_k``, the entry probe halfway between source and stack, the exit
+    probe ``probe_gap`` cells behind the stack.  Layers that would leave less
+    than 20 free cells behind the exit probe are dropped (at least one stays).
+    """
+    rng = np.random.default_rng(seed)
+    ke = rng.integers(ke_range[0], ke_range[1] + 1, size=nruns)
+    offs = [0]
+    ls, le, er, sg = [], [], [], []
+    pin = np.full(nruns, (src_k + stack_start) // 2, dtype=np.int64)
+    pout = np.zeros(nruns, dtype=np.int64)
+    for r in range(nruns):
+        nl = int(rng.integers(layers[0], layers[1] + 1))
+        th = rng.integers(thick[0], thick[1] + 1, size=nl)
+        e = rng.uniform(epsr[0], epsr[1], size=nl)
+        s = rng.uniform(sigma[0], sigma[1], size=nl)
+        pos = stack_start
+        kept = 0
+        for k in range(nl):
+            if kept >= 1 and pos + th[k] + probe_gap + 20 > ke[r]:
+                break
+            ls.append(pos)
+            le.append(pos + int(th[k]))
+            er.append(e[k])
+            sg.append(s[k])
+            pos += int(th[k])
+            kept += 1
+        pout[r] = pos + probe_gap
+        offs.append(len(ls))
+    return SlabBatch(ke.astype(np.int64), np.array(offs, dtype=np.int64), np.array(ls, dtype=np.int64),
+                     np.array(le, dtype=np.int64), np.array(er), np.array(sg), pin, pout, src_k,
+                     dict(seed=seed, nruns=nruns))
+
+
+def plan(ke: np.ndarray, cpt: int, block: int) -> np.ndarray:
+    """Run the library's C++ planner (host only); returns the int32 plan."""
+    lib = _lib.lib()
+    ke32 = np.ascontiguousarray(ke, dtype=np.int32)
+    n = C.c_int(0)
+    rc = lib.fdtd1d_batch_plan(ke32.ctypes.data, ke32.size, cpt, block, None, 0, C.byref(n))
+    if rc:
+        raise _lib.FdtdError(rc, "fdtd1d_batch_plan")
+    out = np.zeros(n.value, dtype=np.int32)
+    rc = lib.fdtd1d_batch_plan(ke32.ctypes.data, ke32.size, cpt, block, out.ctypes.data, out.size, C.byref(n))
+    if rc:
+        raise _lib.FdtdError(rc, "fdtd1d_batch_plan")
+    return out
+
+
+class BatchRunner:
+    """Device-resident inputs of one batch and the launch(es) that run it."""
+
+    def __init__(self, batch: SlabBatch, nsteps: int = 8000, freqs=None, wave=("gauss", 50, 10.0),
+                 device="cuda", tuning=None):
+        self.batch, self.nsteps, self.device = batch, nsteps, torch.device(device)
+        self.freqs = np.linspace(100e6, 3e9, 64) if freqs is None else np.asarray(freqs, dtype=np.float64)
+        nf = self.freqs.size
+        if not 1 <= nf <= 64:
+            raise ValueError("1..64 frequencies")
+        if np.any(batch.probe_in >= batch.ke) or np.any(batch.probe_out >= batch.ke) or batch.src_k >= batch.ke.min():
+            raise ValueError("probe or source cell outside a run")
+        dev = self.device
+        i32 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32)).to(dev)  # noqa: E731
+        self.ke = i32(batch.ke)
+        self.layer_off = i32(batch.layer_off)
+        self.layer_start = i32(batch.layer_start if batch.layer_start.size else np.zeros(1))
+        self.layer_end = i32(batch.layer_end if batch.layer_end.size else np.zeros(1))
+        lca, lcb = layer_coeffs(batch.epsr, batch.sigma) if batch.epsr.size else (np.ones(1), np.ones(1))
+        self.layer_ca, self.layer_cb = to_device(lca, dev), to_device(lcb, dev)
+        self.probe_in, self.probe_out = i32(batch.probe_in), i32(batch.probe_out)
+        self.src_table = to_device(wave_values(wave, 1, nsteps), dev)
+        cs, sn = dft_tables(self.freqs, DT, 1, nsteps)
+        self.dft_cos, self.dft_sin = to_device(cs, dev), to_device(sn, dev)
+        self.spec = torch.zeros((batch.nruns, 4, nf), dtype=torch.float32, device=dev)
+        self.done = torch.zeros(batch.nruns, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._queues = torch.zeros(8, dtype=torch.int32, device=dev)
+        self.tuning = tuning or default_tuning(batch.ke)
+        self._plans = {}
+
+    def _params(self, nsteps: int):
+        p = _lib.BatchParams1D()
+        b = self.batch
+        p.nruns = b.nruns
+        p.ke, p.layer_off = self.ke.data_ptr(), self.layer_off.data_ptr()
+        p.nlayers = int(b.layer_start.size)
+        p.layer_start, p.layer_end = self.layer_start.data_ptr(), self.layer_end.data_ptr()
+        p.layer_ca, p.layer_cb = self.layer_ca.data_ptr(), self.layer_cb.data_ptr()
+        p.probe_in, p.probe_out = self.probe_in.data_ptr(), self.probe_out.data_ptr()
+        p.src_k = b.src_k
+        p.src_table = self.src_table.data_ptr()
+        p.nsteps = nsteps
+        p.nf = self.freqs.size
+        p.dft_cos, p.dft_sin = self.dft_cos.data_ptr(), self.dft_sin.data_ptr()
+        return p
+
+    def _group_plan(self, g: int, runs: np.ndarray, cpt: int, block: int):
+        key = (g, cpt, block, runs.size)
+        if key not in self._plans:
+            pl = plan(self.batch.ke[runs], cpt, block)
+            # the plan numbers runs 0..n-1 within the group: map to batch indices
+            nb = int(pl[0])
+            ent = pl[4 + nb + 1:].reshape(-1, 4)
+            ent[:, 0] = runs[ent[:, 0]]
+            self._plans[key] = (torch.as_tensor(pl).to(self.device), nb, pl.size)
+        return self._plans[key]
+
+    def run(self, nsteps: int | None = None, max_cycles: int = 0) -> None:
+        """Enqueue the whole batch (every group of the tuning) on the current stream."""
+        nsteps = self.nsteps if nsteps is None else nsteps
+        p = self._params(nsteps)
+        st = _lib.stream_ptr()
+        for g, grp in enumerate(self.tuning["groups"]):
+            runs = np.nonzero((self.batch.ke > grp["ke_lo"]) & (self.batch.ke <= grp["ke_hi"]))[0]
+            if runs.size == 0:
+                continue
+            pl, nb, n = self._group_plan(g, runs, grp["cpt"], grp["block"])
+            o = _lib.BatchOut1D()
+            o.spec, o.done, o.status = self.spec.data_ptr(), self.done.data_ptr(), self.status.data_ptr()
+            o.queue = self._queues.data_ptr() + 4 * g
+            _lib.call("fdtd1d_batch_run", C.byref(p), C.byref(o), pl.data_ptr(), n, nb, grp["cpt"], grp["block"],
+                      grp.get("ctas_per_sm", 0), max_cycles, st)
+
+    def transmission(self):
+        """Complex T(f) = DFT_exit/DFT_entry per run, float64 [nruns][nf]."""
+        s = self.spec.double().cpu().numpy()
+        din = s[:, 0] + 1j * s[:, 1]
+        dout = s[:, 2] + 1j * s[:, 3]
+        return dout / din
+
+
+def default_tuning(ke: np.ndarray) -> dict:
+    """Smallest cells-per-thread whose largest block holds the longest run."""
+    kmax = int(np.max(ke))
+    for cpt, block in VARIANTS:
+        if cpt * block >= kmax:
+            return {"groups": [{"ke_lo": 0, "ke_hi": 1 << 30, "cpt": cpt, "block": block}]}
+    raise ValueError(f"runs longer than {VARIANTS[-1][0] * VARIANTS[-1][1]} cells are not supported")
+
+
+def candidate_tunings(ke: np.ndarray):
+    kmax = int(np.max(ke))
+    out = []
+    for cpt, block in VARIANTS:
+        for b in sorted({block, block // 2}):
+            if cpt * b >= kmax:
+                out.append({"groups": [{"ke_lo": 0, "ke_hi": 1 << 30, "cpt": cpt, "block": b}]})
+    # two groups: short runs with few cells per thread, long runs with many
+    for cpt_s, block_s in VARIANTS:
+        for cpt_l, block_l in VARIANTS:
+            cut = cpt_s * block_s
+            if cpt_l * block_l >= kmax and cut < kmax and cpt_s < cpt_l:
+                out.append({"groups": [{"ke_lo": 0, "ke_hi": cut, "cpt": cpt_s, "block": block_s},
+                                       {"ke_lo": cut, "ke_hi": 1 << 30, "cpt": cpt_l, "block": block_l}]})
+    return out
+
+
+def autotune(runner: BatchRunner, probe_steps: int = 400, reps: int = 2, cache: str | None = None) -> dict:
+    """Time every candidate tuning on the first ``probe_steps`` steps; keep the best.
+
+    The block shape (cells per thread, threads per block), the split of runs
+    into groups and so the simulations per SM are chosen here.  Results are
+    cached in ``cache`` (JSON) keyed by the ke distribution.
+    """
+    key = f"{runner.batch.nruns}:{int(runner.batch.ke.sum())}:{int(runner.batch.ke.max())}"
+    if cache and os.path.exists(cache):
+        with open(cache) as fh:
+            d = json.load(fh)
+        if key in d:
+            runner.tuning = d[key]["tuning"]
+            return d[key]
+    results = []
+    for tun in candidate_tunings(runner.batch.ke):
+        runner.tuning = tun
+        runner.run(probe_steps)  # warm-up (plans, module load)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            runner.run(probe_steps)
+        e1.record()
+        torch.cuda.synchronize()
+        results.append((e0.elapsed_time(e1) / reps, tun))
+    results.sort(key=lambda x: x[0])
+    best = {"tuning": results[0][1], "ms_per_probe": results[0][0], "probe_steps": probe_steps,
+            "candidates": [(ms, t) for ms, t in results]}
+    runner.tuning = best["tuning"]
+    if cache:
+        d = {}
+        if os.path.exists(cache):
+            with open(cache) as fh:
+                d = json.load(fh)
+        d[key] = best
+        with open(cache, "w") as fh:
+            json.dump(d, fh)
+    return best

@@ -19,7 +19,7 @@ import sys
 PKG = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
-OUT = os.path.join(PKG, "_build")
+OUT = os.environ.get("FDTD_BUILD_DIR", os.path.join(PKG, "_build"))
 LIB = os.path.join(OUT, "libfdtd_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -53,6 +53,7 @@ def _stamp(flags: list[str]) -> str:
 
 def build(force: bool = False, debug: bool = False, verbose: bool = False) -> str:
     flags = FLAGS + (["-DFDTD_BOUNDS_CHECK"] if debug else [])
+    flags += os.environ.get("FDTD_NVCC_EXTRA", "").split()
     os.makedirs(OUT, exist_ok=True)
     stamp_path = os.path.join(OUT, "stamp.txt")
     stamp = _stamp(flags)

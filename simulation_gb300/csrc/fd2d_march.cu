@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_march(const MarchArgs a) {
 
 // ------------------------------------------------------------- dispatch
 struct MarchConfig {
-  int cpl = 4;
+  int cpl = 0;       // columns per lane; 0 = automatic (measured best: 4 for K <= 2, 2 for K >= 3)
   int warps = 4;
   int seg_rows = 0;  // 0 = automatic
 };
@@ -362,14 +362,15 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
   a.check_finite = status != nullptr;
   const bool lossy = p.nbz != nullptr;
   const bool pml = has_pml(p);
-  if (g_cfg.cpl == 2) return launch_cpl<2>(a, k, lossy, pml, st);
+  const int cpl = g_cfg.cpl ? g_cfg.cpl : (k >= 3 ? 2 : 4);
+  if (cpl == 2) return launch_cpl<2>(a, k, lossy, pml, st);
   return launch_cpl<4>(a, k, lossy, pml, st);
 }
 
 }  // namespace fdtd
 
 extern "C" int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows) {
-  if (cols_per_lane != 2 && cols_per_lane != 4) return FDTD_ERR_ARG;
+  if (cols_per_lane != 0 && cols_per_lane != 2 && cols_per_lane != 4) return FDTD_ERR_ARG;
   if (seg_rows < 0) return FDTD_ERR_ARG;
   fdtd::g_cfg.cpl = cols_per_lane;
   fdtd::g_cfg.warps = warps_per_block;

@@ -120,7 +120,7 @@ def test_segments_and_stripes_bitwise(cuda_lib):
             for k in ("dz", "ez", "iz", "hx", "hy", "ihx", "ihy"):
                 assert torch.equal(getattr(a, k), getattr(b, k)), f"cpl={cpl} seg={seg} {k}"
     finally:
-        _lib.call("fdtd2d_set_march_config", 4, 4, 0)
+        _lib.call("fdtd2d_set_march_config", 0, 4, 0)
 
 
 def test_benchmark_miniature_vs_oracle(cuda_lib):
