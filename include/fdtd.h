@@ -163,6 +163,21 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
  * No reference counterpart. */
 int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows);
 
+/* fdtd2d_step_n without a caller-provided workspace, for callers that cannot
+ * allocate device memory (no cudaMalloc available or allowed where they run).
+ * No counterpart in the reference.  The ping-pong workspace is a static device
+ * array of FDTD2D_NOALLOC_SCRATCH_BYTES inside this library, held by every GPU
+ * that loads it until the process exits; grids needing more (more than
+ * FDTD2D_NOALLOC_MAX_CELLS cells) get FDTD_ERR_SIZE.  Allocates nothing.  The
+ * first call on a device looks the array's address up (cudaGetSymbolAddress):
+ * make it before any stream capture.  All calls share the array (it keeps the
+ * last call's contents, none of which must start at zero); calls that overlap
+ * on the GPU race on it. */
+#define FDTD2D_NOALLOC_MAX_CELLS (1024 * 1024)
+#define FDTD2D_NOALLOC_SCRATCH_BYTES (6ull * 4ull * FDTD2D_NOALLOC_MAX_CELLS)
+int fdtd2d_step_n_noalloc(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass,
+                          fdtd_stream_t stream);
+
 /* Lossy-cylinder material map on the device, float64 arithmetic in the order of
  * dielectric() in fd2d/python/fd2d_3_4.py:174-194 (true division m/3):
  * writes naz, nbz [nx][ny]. */

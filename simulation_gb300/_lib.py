@@ -103,6 +103,7 @@ _SIGS = {
     "fdtd2d_step_n": ([C.POINTER(Params2D), C.POINTER(State2D), C.c_int, C.c_int, C.c_int, P, C.c_size_t, P],
                       C.c_int),
     "fdtd2d_set_march_config": ([C.c_int, C.c_int, C.c_int], C.c_int),
+    "fdtd2d_step_n_noalloc": ([C.POINTER(Params2D), C.POINTER(State2D), C.c_int, C.c_int, C.c_int, P], C.c_int),
     "fdtd2d_dielectric_cylinder": ([C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     F, F, P], C.c_int),
     "fdtd_check_finite": ([F, C.c_size_t, P, P], C.c_int),

@@ -1,0 +1,80 @@
+// fdtd2d_step_n_noalloc: the fused 2D time loop for callers that cannot
+// allocate device memory.
+//
+// Who needs it: code that runs where cudaMalloc is unavailable or forbidden
+// (a host application with a fixed memory budget that pre-reserves
+// everything, a plugin called inside another framework's stream capture or
+// memory pool, an embedded runtime without an allocator of its own).  Such a
+// caller still owns the field arrays but cannot provide the ping-pong
+// workspace fdtd2d_step_n needs.
+//
+// What it does: the workspace is a file-scope static device array of
+// FDTD2D_NOALLOC_SCRATCH_BYTES (24 MiB: six fields of up to
+// FDTD2D_NOALLOC_MAX_CELLS = 1024*1024 cells).  Every GPU that loads this
+// library holds that array until the process exits.  The call allocates
+// nothing (no cudaMalloc/cudaFree, no allocating library routine): it looks
+// the array's device address up once per device and hands it to
+// fdtd2d_step_n as the workspace.  Everything else is fdtd2d_step_n's code
+// path, unchanged.
+//
+// Limits and caveats (also in include/fdtd.h):
+//   * grids whose workspace exceeds the array are rejected with FDTD_ERR_SIZE;
+//   * the first call on a device resolves the array's address with
+//     cudaGetSymbolAddress; make that first call before any stream capture;
+//   * all calls share the one array and it keeps the last call's contents;
+//     nothing in it has to start at zero (each call's first pass overwrites
+//     it before reading it), but calls whose work overlaps on the GPU (two
+//     streams, two host threads) race on it.
+#include <mutex>
+
+#include "fdtd_common.cuh"
+
+namespace {
+
+constexpr size_t kScratchBytes = (size_t)FDTD2D_NOALLOC_SCRATCH_BYTES;
+
+// the workspace; only device code may name it directly, host code must use the
+// address returned by cudaGetSymbolAddress (the host-side symbol is a stand-in)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_addr[kMaxDevices] = {nullptr};
+
+int scratch_address(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    fdtd_host::note_cuda_error(e);
+    return FDTD_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kMaxDevices) return FDTD_ERR_UNSUPPORTED;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      fdtd_host::note_cuda_error(e);
+      return FDTD_ERR_CUDA;
+    }
+    g_addr[dev] = p;
+  }
+  *out = g_addr[dev];
+  return FDTD_OK;
+}
+
+}  // namespace
+
+extern "C" int fdtd2d_step_n_noalloc(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps,
+                                     int steps_per_pass, fdtd_stream_t stream) {
+  if (!p || !s) return FDTD_ERR_NULL;
+  if ((long long)p->nx * p->ny > (long long)FDTD2D_NOALLOC_MAX_CELLS) return FDTD_ERR_SIZE;
+  const size_t need = fdtd2d_workspace_size(p, steps_per_pass);
+  if (need > kScratchBytes) return FDTD_ERR_SIZE;
+  void* ws = nullptr;
+  if (need > 0) {
+    const int rc = scratch_address(&ws);
+    if (rc != FDTD_OK) return rc;
+  }
+  return fdtd2d_step_n(p, s, t0, nsteps, steps_per_pass, ws, need > 0 ? kScratchBytes : 0, stream);
+}
