@@ -46,9 +46,11 @@ METRIC = "Gcell-updates/s & %HBM peak; surrogate vs FDTD spectra/s at ≤1% L2 e
 UNIT = "Gcell-updates/s"
 WORKLOAD = ("2D TM PML lossy-cylinder benchmark program: 8192x8192, npml=32 grade 0.333, "
             "cylinder r=1000 eps_r=30 sigma=0.3, hard Gaussian Dz source t0=20 spread=6, 2000 steps, FP32")
-# DRAM bytes per cell per fused pass from the ncu capture of the fused kernel
-# (dram__bytes_read.sum + dram__bytes_write.sum / cells); None until captured
-NCU_TRAFFIC_BYTES_PER_CELL_PASS: float | None = None
+# DRAM bytes per cell per fused K=4 pass, from one ncu capture of the fused kernel
+# on the 4096^2 case ((dram__bytes_read.sum + dram__bytes_write.sum) / cells =
+# 998.35 MB / 16.78 M cells, profiles/k_march_K4_CPL2_full_4096.md); traffic
+# grows in proportion to the cells, so it is scaled to the launch size
+NCU_TRAFFIC_BYTES_PER_CELL_PASS = {4: 59.5}
 
 
 def _peaks():
@@ -161,7 +163,7 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     import numpy as np  # noqa: F401
-    steps_per_sample = int(os.environ.get("FDTD_REF_SAMPLE_STEPS", "4"))
+    steps_per_sample = int(os.environ.get("FDTD_REF_SAMPLE_STEPS", "20"))
     for _ in range(args.warmup):
         cpu_port_rate(NX, NY, 1)
     vals = []
@@ -247,16 +249,23 @@ def run_ours(args) -> None:
     peak, peak_kind = _peaks()
     algo_bytes = BYTES_PER_CELL_UPDATE * cells * spp
     achieved = algo_bytes / (pass_ms / 1e3) / 1e9
-    traffic = None if NCU_TRAFFIC_BYTES_PER_CELL_PASS is None else NCU_TRAFFIC_BYTES_PER_CELL_PASS * cells
+    tb = NCU_TRAFFIC_BYTES_PER_CELL_PASS.get(spp)
+    traffic = None if tb is None else tb * cells
 
     # e2e through the public API with host buffers
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(sim, args, st, world, dev)
 
+    extra = None
+    if rank == 0 and not args.no_extra:
+        del sim
+        torch.cuda.empty_cache()
+        extra = run_secondary(args, st, world)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS", "8")))
+        cpu = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS", "150")))
         cpu["unit"] = UNIT
         cpu["kind"] = "port"
 
@@ -274,10 +283,52 @@ def run_ours(args) -> None:
                              "kernel": f"k_march<K={spp}> (one fused pass = {spp} time steps)",
                              "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": pass_ms},
                 "e2e": e2e, "cpu_baseline": cpu, "clocks": clocks,
-                "gpu_launches": passes_per_run * args.steps}
+                "gpu_launches": passes_per_run * args.steps, "secondary_workloads": extra}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def run_secondary(args, st, world) -> dict:
+    """The other workloads of the path, measured after the headline (not part of `value`)."""
+    import numpy as np
+    import torch
+
+    from simulation_gb300 import batch1d as B
+    from simulation_gb300 import fd1d as G1
+    out = {}
+    # plain 1D dielectric case: ke=200, hard source at k=5, 1000 steps, one fused launch
+    sim = G1.program("config1", ns=1000)
+    for _ in range(5):
+        sim.t = 0
+        sim.step(1000)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(20):
+        sim.t = 0
+        sim.step(1000)
+    e1.record(st)
+    torch.cuda.synchronize()
+    us = e0.elapsed_time(e1) * 1e3 / 20
+    out["fd1d_dielectric_ke200_1000steps"] = {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3,
+                                              "kernel_launches_per_run": 1}
+    # batched uneven 1D slab runs: 4096 runs, ke ~ U[500,20000], 8000 steps, 64-frequency probes
+    batch = B.slab_batch(4096, seed=0)
+    runner = B.BatchRunner(batch, nsteps=8000)
+    tuned = B.autotune(runner, probe_steps=400, reps=1)
+    runner.run()
+    torch.cuda.synchronize()
+    e0.record(st)
+    runner.run()
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = int(batch.ke.sum()) * 8000
+    out["batch1d_4096_slabs_8000steps"] = {"ms": ms, "Gcell_updates_per_s": cells / ms / 1e6,
+                                           "spectra_per_s": batch.nruns / ms * 1e3, "tuning": tuned["tuning"],
+                                           "status": int(runner.status.item()),
+                                           "runs_done": int(runner.done.sum().item())}
+    return out
 
 
 def run_e2e(sim, args, st, world, dev) -> dict:
@@ -327,6 +378,7 @@ def main():
     ap.add_argument("--ns", type=int, default=2000, help="time steps per bench step")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
     args = ap.parse_args()
     global NX, NY, NS
     NX = NY = args.grid
