@@ -113,6 +113,10 @@ typedef struct {
   const float* dft_cos; /* device [table_len][nf]: cos(2*pi*f*dt*t) at row t-1 */
   const float* dft_sin; /* device [table_len][nf] */
   int dft_table_len;
+  /* Ez recorded at one cell every step (state.probe_ez, NULL = off):
+   * probe_ez[t-1] = ez[probe_i][probe_j] after step t; probe_len entries */
+  int probe_i, probe_j;
+  int probe_len;
 } fdtd2d_params;
 
 typedef struct {
@@ -121,6 +125,7 @@ typedef struct {
   float *r_pt, *i_pt;                        /* DFT [nf][nx][ny] */
   float *r_in, *i_in;                        /* DFT of ezi[6], [nf] */
   int* status;                               /* device status word, may be NULL */
+  float* probe_ez;                           /* device [probe_len] Ez trace at the probe cell, or NULL */
 } fdtd2d_state;
 
 /* dfield: D update + point source (+ ezi[3] for TF/SF) for step t.
@@ -177,6 +182,34 @@ int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows
 #define FDTD2D_NOALLOC_SCRATCH_BYTES (6ull * 4ull * FDTD2D_NOALLOC_MAX_CELLS)
 int fdtd2d_step_n_noalloc(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass,
                           fdtd_stream_t stream);
+
+/* ------------------------------------------------ differentiation (adjoint)
+ * No counterpart in the reference (it only runs forward).  A reverse sweep
+ * over checkpoints: restore a checkpoint, recompute the states of its segment
+ * with fdtd2d_pass, then walk the segment backwards with fdtd2d_adjoint_step. */
+typedef struct {
+  float *dz, *iz, *hx, *hy, *ihx, *ihy; /* [nx][ny] each; iz NULL if lossless */
+} fdtd2d_fields;
+
+typedef struct {
+  int i0, j0, ni, nj; /* design box: rows i0..i0+ni-1, columns j0..j0+nj-1 */
+} fdtd2d_box;
+
+/* One out-of-place fused pass: the fields after steps t0+1..t0+k (k = 1..4)
+ * of `in` go to `out`, Ez to `ez` (same kernel and results as fdtd2d_step_n;
+ * point source only, ny % 4 == 0, 16-byte aligned buffers). */
+int fdtd2d_pass(const fdtd2d_params* p, const fdtd2d_fields* in, fdtd2d_fields* out, float* ez, int t0, int k,
+                int* status, fdtd_stream_t stream);
+
+/* Reverse of time step t of the lossy PML update (fd2d/python/fd2d_3_2.py:62-88
+ * with fd2d/python/fd2d_3_4.py:131-136) for J = sum_t (probe_weight/2)*ez_t[probe]^2:
+ * `fwd` is the state BEFORE step t; `adj` holds the adjoints of the state after
+ * step t and receives those before it (in place); `adj_tmp` is [nx][ny]
+ * scratch.  Adds dJ/dnaz (and dJ/dnbz if non-NULL) over `box` into grad_naz
+ * [ni][nj].  Needs the ten PML vectors (unit profiles for no layer). */
+int fdtd2d_adjoint_step(int t, const fdtd2d_params* p, const fdtd2d_fields* fwd, fdtd2d_fields* adj, float* adj_tmp,
+                        int probe_i, int probe_j, float probe_weight, fdtd2d_box box, float* grad_naz,
+                        float* grad_nbz, fdtd_stream_t stream);
 
 /* Lossy-cylinder material map on the device, float64 arithmetic in the order of
  * dielectric() in fd2d/python/fd2d_3_4.py:174-194 (true division m/3):

@@ -55,12 +55,21 @@ class Source2D(C.Structure):
 class Params2D(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("pml", Pml2D), ("naz", F), ("nbz", F), ("src", Source2D),
                 ("tfsf_npml", C.c_int), ("tfsf_table", F), ("tfsf_table_len", C.c_int),
-                ("nf", C.c_int), ("dft_cos", F), ("dft_sin", F), ("dft_table_len", C.c_int)]
+                ("nf", C.c_int), ("dft_cos", F), ("dft_sin", F), ("dft_table_len", C.c_int),
+                ("probe_i", C.c_int), ("probe_j", C.c_int), ("probe_len", C.c_int)]
 
 
 class State2D(C.Structure):
     _fields_ = [(n, F) for n in ("dz", "ez", "iz", "hx", "hy", "ihx", "ihy", "ezi", "hxi", "bc",
-                                 "r_pt", "i_pt", "r_in", "i_in")] + [("status", P)]
+                                 "r_pt", "i_pt", "r_in", "i_in")] + [("status", P), ("probe_ez", F)]
+
+
+class Fields2D(C.Structure):
+    _fields_ = [(n, F) for n in ("dz", "iz", "hx", "hy", "ihx", "ihy")]
+
+
+class Box2D(C.Structure):
+    _fields_ = [("i0", C.c_int), ("j0", C.c_int), ("ni", C.c_int), ("nj", C.c_int)]
 
 
 class Params1D(C.Structure):
@@ -103,6 +112,10 @@ _SIGS = {
     "fdtd2d_step_n": ([C.POINTER(Params2D), C.POINTER(State2D), C.c_int, C.c_int, C.c_int, P, C.c_size_t, P],
                       C.c_int),
     "fdtd2d_set_march_config": ([C.c_int, C.c_int, C.c_int], C.c_int),
+    "fdtd2d_pass": ([C.POINTER(Params2D), C.POINTER(Fields2D), C.POINTER(Fields2D), F, C.c_int, C.c_int, P, P],
+                    C.c_int),
+    "fdtd2d_adjoint_step": ([C.c_int, C.POINTER(Params2D), C.POINTER(Fields2D), C.POINTER(Fields2D), F, C.c_int,
+                             C.c_int, C.c_float, Box2D, F, F, P], C.c_int),
     "fdtd2d_step_n_noalloc": ([C.POINTER(Params2D), C.POINTER(State2D), C.c_int, C.c_int, C.c_int, P], C.c_int),
     "fdtd2d_dielectric_cylinder": ([C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     F, F, P], C.c_int),

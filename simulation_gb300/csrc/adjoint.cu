@@ -1,0 +1,207 @@
+// Reverse-time (adjoint) step of the lossy 2D TM update with PML, and the
+// out-of-place fused pass used to recompute forward states between checkpoints.
+//
+// No counterpart in the reference (which only runs forward); the forward map
+// being differentiated is the reference's step, fd2d/python/fd2d_3_2.py:62-88
+// with the lossy E update of fd2d/python/fd2d_3_4.py:131-136 and a point
+// source after the D update.
+//
+// Forward step t maps x = (dz, iz, hx, hy, ihx, ihy) to x':
+//   dz' = ca*dz + cb*curl(hy, hx)       ca = gx3*gy3, cb = 0.5*gx2*gy2  (i, j >= 1)
+//   dz'[src] = v (hard) or += v (soft)
+//   ez  = naz*(dz' - iz);  iz' = iz + nbz*ez
+//   cx = ez - ez[j+1], cy = ez - ez[i+1];  ihx' = ihx + cx;  ihy' = ihy + cy
+//   hx' = fy3*hx + fy2*(0.5*cx + fx1*ihx');  hy' = fx3*hy - fx2*(0.5*cy + fy1*ihy')
+// and the objective adds w/2 * ez[probe]^2 per step (J = sum ez^2 for w = 2).
+// Given the adjoints L' of x' this computes the adjoints L of x and adds
+// dJ/dnaz, dJ/dnbz on a design box.  Two kernels, because L(dz) at a cell
+// needs L'(dz) of its +i and +j neighbours after they received their E terms:
+//   A: recompute dz', ez at the cell from x; L(ez) from the H adjoints of the
+//      cell and its (i, j-1), (i-1, j) neighbours (+ probe seed); E backward;
+//      writes L'(dz)+E terms to a temporary and L(iz) in place; gradients;
+//   B: D backward: L(dz) = ca*T, L(hy) += cb*T - cb[i+1]*T[i+1],
+//      L(hx) += -cb*T + cb[j+1]*T[j+1]; H backward for hx, hy, ihx, ihy.
+#include "fd2d_internal.cuh"
+
+namespace fdtd {
+
+namespace {
+
+struct AdjArgs {
+  int nx, ny, t;
+  fdtd2d_pml pml;
+  const float* naz;
+  const float* nbz;
+  int src_kind, src_i, src_j;
+  const float* src_table;
+  fdtd2d_fields fwd;  // state before step t
+  fdtd2d_fields adj;  // adjoints: after step t in, before step t out
+  float* tmp;
+  int probe_i, probe_j;
+  float probe_w;
+  fdtd2d_box box;
+  float* grad_naz;
+  float* grad_nbz;
+};
+
+__device__ __forceinline__ float lam_cx(const AdjArgs& a, int i, int j) {
+  // adjoint of cx at (i, j) from hx', ihx' there (0 where H is not applied)
+  if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
+  const size_t n = (size_t)i * a.ny + j;
+  const float lhx = a.adj.hx[n];
+  const float fy2 = __ldg(a.pml.fy2 + j);
+  const float lihx_t = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, a.adj.ihx[n]);
+  return __fmaf_rn(__fmul_rn(0.5f, fy2), lhx, lihx_t);
+}
+
+__device__ __forceinline__ float lam_cy(const AdjArgs& a, int i, int j) {
+  if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
+  const size_t n = (size_t)i * a.ny + j;
+  const float lhy = a.adj.hy[n];
+  const float fx2 = __ldg(a.pml.fx2 + i);
+  const float lihy_t = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, a.adj.ihy[n]);
+  return __fmaf_rn(-__fmul_rn(0.5f, fx2), lhy, lihy_t);
+}
+
+__global__ void k_adj_a(const AdjArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  // forward recompute of dz' and ez at this cell (same formulas as the forward)
+  float dzp = a.fwd.dz[n];
+  if (i >= 1 && j >= 1)
+    dzp = d_update(dzp, a.fwd.hy[n], a.fwd.hy[n - a.ny], a.fwd.hx[n], a.fwd.hx[n - 1], __ldg(a.pml.gx3 + i),
+                   __ldg(a.pml.gy3 + j), __ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j));
+  if (a.src_kind != FDTD_SRC_NONE && i == a.src_i && j == a.src_j) {
+    const float v = __ldg(a.src_table + a.t - 1);
+    dzp = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(dzp, v);
+  }
+  const float izv = a.nbz ? a.fwd.iz[n] : 0.f;
+  const float diff = __fsub_rn(dzp, izv);
+  const float naz = __ldg(a.naz + n);
+  const float ez = __fmul_rn(naz, diff);
+  // adjoint of ez
+  float lez = lam_cx(a, i, j) - lam_cx(a, i, j - 1) + lam_cy(a, i, j) - lam_cy(a, i - 1, j);
+  if (i == a.probe_i && j == a.probe_j) lez = __fmaf_rn(a.probe_w, ez, lez);
+  // E backward
+  const float nbz = a.nbz ? __ldg(a.nbz + n) : 0.f;
+  const float liz = a.nbz ? a.adj.iz[n] : 0.f;
+  const float lezt = __fmaf_rn(nbz, liz, lez);
+  a.tmp[n] = __fmaf_rn(naz, lezt, a.adj.dz[n]);
+  if (a.nbz) a.adj.iz[n] = __fmaf_rn(-naz, lezt, liz);
+  const int bi = i - a.box.i0, bj = j - a.box.j0;
+  if (a.grad_naz && bi >= 0 && bi < a.box.ni && bj >= 0 && bj < a.box.nj) {
+    const size_t b = (size_t)bi * a.box.nj + bj;
+    a.grad_naz[b] = __fmaf_rn(lezt, diff, a.grad_naz[b]);
+    if (a.grad_nbz) a.grad_nbz[b] = __fmaf_rn(liz, ez, a.grad_nbz[b]);
+  }
+}
+
+// cb*T at (i, j): the D adjoint flowing into the curl's H terms (0 where D is
+// not applied, or at a hard source whose dz' does not depend on the state)
+__device__ __forceinline__ float dgrad(const AdjArgs& a, int i, int j) {
+  if (i < 1 || j < 1 || i >= a.nx || j >= a.ny) return 0.f;
+  if (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j) return 0.f;
+  const float cb = __fmul_rn(__fmul_rn(__ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j)), 0.5f);
+  return __fmul_rn(cb, a.tmp[(size_t)i * a.ny + j]);
+}
+
+__global__ void k_adj_b(const AdjArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const bool hard_src = (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j);
+  const float T = a.tmp[n];
+  float ldz;
+  if (hard_src) ldz = 0.f;
+  else if (i >= 1 && j >= 1) ldz = __fmul_rn(__fmul_rn(__ldg(a.pml.gx3 + i), __ldg(a.pml.gy3 + j)), T);
+  else ldz = T;
+  const float dg = dgrad(a, i, j);
+  const bool hm = (i <= a.nx - 2) && (j <= a.ny - 2);
+  float lhx = a.adj.hx[n], lhy = a.adj.hy[n], lihx = a.adj.ihx[n], lihy = a.adj.ihy[n];
+  if (hm) {
+    const float fy2 = __ldg(a.pml.fy2 + j), fx2 = __ldg(a.pml.fx2 + i);
+    lihx = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, lihx);
+    lihy = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, lihy);
+    lhx = __fmul_rn(__ldg(a.pml.fy3 + j), lhx);
+    lhy = __fmul_rn(__ldg(a.pml.fx3 + i), lhy);
+  }
+  lhy = __fadd_rn(__fadd_rn(lhy, dg), -dgrad(a, i + 1, j));
+  lhx = __fadd_rn(__fsub_rn(lhx, dg), dgrad(a, i, j + 1));
+  a.adj.dz[n] = ldz;
+  a.adj.hx[n] = lhx;
+  a.adj.hy[n] = lhy;
+  a.adj.ihx[n] = lihx;
+  a.adj.ihy[n] = lihy;
+}
+
+}  // namespace
+
+}  // namespace fdtd
+
+extern "C" {
+
+int fdtd2d_pass(const fdtd2d_params* p, const fdtd2d_fields* in, fdtd2d_fields* out, float* ez, int t0, int k,
+                int* status, fdtd_stream_t stream) {
+  if (!p || !in || !out || !ez) return FDTD_ERR_NULL;
+  if (p->nx < 3 || p->ny < 3 || p->ny % 4) return FDTD_ERR_SIZE;
+  if (k < 1 || k > fdtd::march_max_steps_per_pass() || t0 < 0) return FDTD_ERR_ARG;
+  if (!in->dz || !in->hx || !in->hy || !out->dz || !out->hx || !out->hy || !p->naz) return FDTD_ERR_NULL;
+  if (p->nbz && (!in->iz || !out->iz)) return FDTD_ERR_NULL;
+  if (fdtd::has_pml(*p) && (!in->ihx || !in->ihy || !out->ihx || !out->ihy)) return FDTD_ERR_NULL;
+  if (p->src.kind != FDTD_SRC_NONE && (!p->src.table || t0 + k > p->src.table_len)) return FDTD_ERR_SIZE;
+  if (p->tfsf_npml > 0 || p->nf > 0) return FDTD_ERR_UNSUPPORTED;
+  if (in->dz == out->dz) return FDTD_ERR_ARG;
+  fdtd::FieldSet fi{in->dz, in->iz, in->hx, in->hy, in->ihx, in->ihy};
+  fdtd::FieldSet fo{out->dz, out->iz, out->hx, out->hy, out->ihx, out->ihy};
+  return fdtd::launch_march(*p, fi, fo, ez, t0, k, status, nullptr, (cudaStream_t)stream);
+}
+
+int fdtd2d_adjoint_step(int t, const fdtd2d_params* p, const fdtd2d_fields* fwd, fdtd2d_fields* adj, float* adj_tmp,
+                        int probe_i, int probe_j, float probe_weight, fdtd2d_box box, float* grad_naz,
+                        float* grad_nbz, fdtd_stream_t stream) {
+  if (!p || !fwd || !adj || !adj_tmp) return FDTD_ERR_NULL;
+  if (p->nx < 3 || p->ny < 3) return FDTD_ERR_SIZE;
+  if (t < 1) return FDTD_ERR_ARG;
+  if (!fdtd::has_pml(*p)) return FDTD_ERR_UNSUPPORTED;  // pass unit profiles for no absorbing layer
+  if (!p->naz || !fwd->dz || !fwd->hx || !fwd->hy) return FDTD_ERR_NULL;
+  if (!adj->dz || !adj->hx || !adj->hy || !adj->ihx || !adj->ihy) return FDTD_ERR_NULL;
+  if (p->nbz && (!fwd->iz || !adj->iz)) return FDTD_ERR_NULL;
+  if (p->src.kind != FDTD_SRC_NONE && (!p->src.table || t > p->src.table_len)) return FDTD_ERR_SIZE;
+  if (p->tfsf_npml > 0 || p->nf > 0) return FDTD_ERR_UNSUPPORTED;
+  if (grad_naz && (box.ni <= 0 || box.nj <= 0 || box.i0 < 0 || box.j0 < 0 || box.i0 + box.ni > p->nx ||
+                   box.j0 + box.nj > p->ny))
+    return FDTD_ERR_ARG;
+  fdtd::AdjArgs a{};
+  a.nx = p->nx;
+  a.ny = p->ny;
+  a.t = t;
+  a.pml = p->pml;
+  a.naz = p->naz;
+  a.nbz = p->nbz;
+  a.src_kind = p->src.kind;
+  a.src_i = p->src.i;
+  a.src_j = p->src.j;
+  a.src_table = p->src.table;
+  a.fwd = *fwd;
+  a.adj = *adj;
+  a.tmp = adj_tmp;
+  a.probe_i = probe_i;
+  a.probe_j = probe_j;
+  a.probe_w = probe_weight;
+  a.box = box;
+  a.grad_naz = grad_naz;
+  a.grad_nbz = grad_nbz;
+  const dim3 blk(32, 8);
+  const dim3 grd((p->ny + 31) / 32, (p->nx + 7) / 8);
+  cudaStream_t st = (cudaStream_t)stream;
+  fdtd::k_adj_a<<<grd, blk, 0, st>>>(a);
+  int rc = fdtd_host::check_launch();
+  if (rc) return rc;
+  fdtd::k_adj_b<<<grd, blk, 0, st>>>(a);
+  return fdtd_host::check_launch();
+}
+
+}  // extern "C"

@@ -41,6 +41,10 @@ int check_params(const fdtd2d_params* p, const fdtd2d_state* s, int t_last, bool
     if (p->tfsf_npml > 0 && (!s->r_in || !s->i_in)) return FDTD_ERR_NULL;
     if (t_last > p->dft_table_len) return FDTD_ERR_SIZE;
   }
+  if (s->probe_ez) {
+    if (p->probe_i < 0 || p->probe_i >= p->nx || p->probe_j < 0 || p->probe_j >= p->ny) return FDTD_ERR_ARG;
+    if (t_last > p->probe_len) return FDTD_ERR_SIZE;
+  }
   (void)need_e;
   return FDTD_OK;
 }
@@ -72,6 +76,14 @@ int step_per_function(int t, const fdtd2d_params& p, const fdtd2d_state& s, cuda
   if ((rc = launch_dfield(t, p, s, st))) return rc;
   if (tfsf && (rc = launch_inctdz(p, s, st))) return rc;
   if ((rc = launch_efield(p, s, st))) return rc;
+  if (s.probe_ez) {
+    const cudaError_t e = cudaMemcpyAsync(s.probe_ez + (t - 1), s.ez + (size_t)p.probe_i * p.ny + p.probe_j,
+                                          sizeof(float), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) {
+      fdtd_host::note_cuda_error(e);
+      return FDTD_ERR_CUDA;
+    }
+  }
   if (p.nf > 0 && (rc = launch_fourier(t, p, s, st))) return rc;
   if (tfsf && (rc = launch_hxinct(p, s, st))) return rc;
   if ((rc = launch_hfield(p, s, st))) return rc;
@@ -209,7 +221,7 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
   for (size_t i = 0; i < sched.size(); ++i) {
     const FieldSet& in = (i % 2 == 0) ? user : ws;
     const FieldSet& out = (i % 2 == 0) ? ws : user;
-    if ((rc = launch_march(*p, in, out, s->ez, t, sched[i], s->status, st))) return rc;
+    if ((rc = launch_march(*p, in, out, s->ez, t, sched[i], s->status, s->probe_ez, st))) return rc;
     t += sched[i];
   }
   if (copy_back) {

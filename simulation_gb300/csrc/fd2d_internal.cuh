@@ -30,7 +30,7 @@ struct FieldSet {
   float *dz, *iz, *hx, *hy, *ihx, *ihy;
 };
 int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out, float* ez, int t0, int k,
-                 int* status, cudaStream_t st);
+                 int* status, float* probe_ez, cudaStream_t st);
 // columns a warp of the fused kernel owns (for workspace/grid sizing)
 int march_max_steps_per_pass();
 

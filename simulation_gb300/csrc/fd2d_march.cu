@@ -55,6 +55,8 @@ struct MarchArgs {
   int seg_rows, n_stripes, n_segs;
   int* status;
   int check_finite;
+  int probe_i, probe_j;  // Ez trace cell (probe_ez != nullptr)
+  float* probe_ez;       // probe_ez[t-1] = ez at the probe after step t
 };
 
 template <int CPL>
@@ -203,6 +205,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_march(const MarchArgs a) {
         nd[c] = d;
         niz[c] = izv;
         ne[c] = e;
+        // the probe cell's Ez is recorded by the warp that owns it (output
+        // column, row inside the segment), where every level is valid
+        if (a.probe_ez && q == a.probe_i && j == a.probe_j && vout && q >= i_s && q < i_e)
+          a.probe_ez[a.t0 + s] = e;
       }
 
       // ---- H on row qc (needs Ez of rows qc and q at this level)
@@ -343,7 +349,7 @@ int launch_cpl(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st)
 int march_max_steps_per_pass() { return HALO; }
 
 int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out, float* ez, int t0, int k,
-                 int* status, cudaStream_t st) {
+                 int* status, float* probe_ez, cudaStream_t st) {
   MarchArgs a{};
   a.nx = p.nx;
   a.ny = p.ny;
@@ -360,6 +366,9 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
   a.t0 = t0;
   a.status = status;
   a.check_finite = status != nullptr;
+  a.probe_i = p.probe_i;
+  a.probe_j = p.probe_j;
+  a.probe_ez = probe_ez;
   const bool lossy = p.nbz != nullptr;
   const bool pml = has_pml(p);
   const int cpl = g_cfg.cpl ? g_cfg.cpl : (k >= 3 ? 2 : 4);
