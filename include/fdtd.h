@@ -211,6 +211,62 @@ int fdtd2d_adjoint_step(int t, const fdtd2d_params* p, const fdtd2d_fields* fwd,
                         int probe_i, int probe_j, float probe_weight, fdtd2d_box box, float* grad_naz,
                         float* grad_nbz, fdtd_stream_t stream);
 
+/* ------------------------------------------------ BF16 tensor-core GEMM
+ * D = epilogue(alpha * A.B) on sm_103a tensor cores (tcgen05, TMA, TMEM),
+ * FP32 accumulation; used by the neural-operator surrogate (no reference
+ * counterpart).  A is [M][K] (K-major, lda >= K) or stored transposed [K][M]
+ * (a_mn_major, lda >= M); B is [N][K] (K-major, D = A.B^T) or [K][N]
+ * (b_mn_major, D = A.B).  BF16 operands, 16-byte aligned, leading dimensions
+ * multiples of 8.  Epilogue: z = alpha*acc + bias[n] + res16[m][n];
+ * pre16 = z (optional); y = act ? gelu(z) : z; y += C (accumulate); C = y as
+ * FP32 (C32) or BF16 (C16).  `batch` independent products with element strides. */
+typedef struct {
+  int M, N, K, batch;
+  const void* A;
+  long long lda, stride_a;
+  int a_mn_major;
+  const void* B;
+  long long ldb, stride_b;
+  int b_mn_major;
+  float* C32;
+  void* C16;
+  long long ldc, stride_c;
+  const float* bias;
+  const void* res16;
+  long long ldr, stride_r;
+  float alpha;
+  int act; /* 0 none, 1 GELU (erf form) */
+  int accumulate;
+  void* pre16;
+  int mn_lbo, mn_sbo; /* descriptor byte offsets for MN-major tiles (0 = default) */
+} fdtd_gemm_desc;
+
+int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_t stream);
+
+/* ------------------------------------------------ surrogate helper kernels
+ * Element-wise/reduction pieces of the 1D Fourier-neural-operator surrogate
+ * (no reference counterpart); BF16 tensors are passed as void*.  Shapes:
+ * rows = B*N positions, C channels, M retained modes, DFT layout [B][C][2M]
+ * (cos rows, then -sin rows), mode-major layout [M][B][2C] ([Re | Im]). */
+int fno_lift_fwd(long long rows, int C, const float* in, const float* P, const float* p, void* x0,
+                 fdtd_stream_t stream);
+int fno_lift_bwd(long long rows, int C, const float* in, const void* dx0, float* dP, float* dp,
+                 fdtd_stream_t stream);
+int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_t stream);
+int fno_modes_to_dft(int B, int C, int M, const float* Gm, void* G, fdtd_stream_t stream);
+int fno_build_rbig(int M, int C, const float* Rr, const float* Ri, void* Rbig, fdtd_stream_t stream);
+int fno_fold_drbig(int M, int C, const float* dRbig, float* dRr, float* dRi, fdtd_stream_t stream);
+int fno_gelu_fwd(long long n, const float* z, void* y, void* pre, fdtd_stream_t stream);
+int fno_gelu_bwd(long long n, const void* dy16, const float* dy32, const void* pre, void* dz, fdtd_stream_t stream);
+int fno_meanpool(int B, int N, int C, const void* x, void* h, fdtd_stream_t stream);
+int fno_meanpool_bwd(int B, int N, int C, const float* dh, void* dx, fdtd_stream_t stream);
+int fno_colsum(long long rows, int C, const void* x16, const float* x32, float* out, fdtd_stream_t stream);
+int fno_sum_parts(int nb, long long n, const float* parts, float* out, fdtd_stream_t stream);
+int fno_mse(int B, int D, const float* o, const float* y, float* dO, float* loss, fdtd_stream_t stream);
+int fno_adam(long long n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
+             int step, void* w16, fdtd_stream_t stream);
+int fno_to_bf16(long long n, const float* x, void* y, fdtd_stream_t stream);
+
 /* Lossy-cylinder material map on the device, float64 arithmetic in the order of
  * dielectric() in fd2d/python/fd2d_3_4.py:174-194 (true division m/3):
  * writes naz, nbz [nx][ny]. */

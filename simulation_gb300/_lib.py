@@ -72,6 +72,16 @@ class Box2D(C.Structure):
     _fields_ = [("i0", C.c_int), ("j0", C.c_int), ("ni", C.c_int), ("nj", C.c_int)]
 
 
+class GemmDesc(C.Structure):
+    _fields_ = [("M", C.c_int), ("N", C.c_int), ("K", C.c_int), ("batch", C.c_int),
+                ("A", P), ("lda", C.c_longlong), ("stride_a", C.c_longlong), ("a_mn_major", C.c_int),
+                ("B", P), ("ldb", C.c_longlong), ("stride_b", C.c_longlong), ("b_mn_major", C.c_int),
+                ("C32", P), ("C16", P), ("ldc", C.c_longlong), ("stride_c", C.c_longlong),
+                ("bias", P), ("res16", P), ("ldr", C.c_longlong), ("stride_r", C.c_longlong),
+                ("alpha", C.c_float), ("act", C.c_int), ("accumulate", C.c_int), ("pre16", P),
+                ("mn_lbo", C.c_int), ("mn_sbo", C.c_int)]
+
+
 class Params1D(C.Structure):
     _fields_ = [("nx", C.c_int), ("form", C.c_int)] + [(n, F) for n in ("ca", "cb", "nax", "nbx", "ncx", "ndx")] + [
         ("src_kind", C.c_int), ("src_k", C.c_int), ("src_table", F), ("src_table_len", C.c_int),
@@ -124,6 +134,22 @@ _SIGS = {
     "fdtd1d_hfield": ([C.POINTER(Params1D), C.POINTER(State1D), P], C.c_int),
     "fdtd1d_fourier": ([C.c_int, C.POINTER(Params1D), C.POINTER(State1D), P], C.c_int),
     "fdtd1d_step_n": ([C.POINTER(Params1D), C.POINTER(State1D), C.c_int, C.c_int, P], C.c_int),
+    "fdtd_gemm_bf16": ([C.POINTER(GemmDesc), P, P], C.c_int),
+    "fno_lift_fwd": ([C.c_longlong, C.c_int, F, F, F, P, P], C.c_int),
+    "fno_lift_bwd": ([C.c_longlong, C.c_int, F, P, F, F, P], C.c_int),
+    "fno_dft_to_modes": ([C.c_int, C.c_int, C.c_int, F, P, P], C.c_int),
+    "fno_modes_to_dft": ([C.c_int, C.c_int, C.c_int, F, P, P], C.c_int),
+    "fno_build_rbig": ([C.c_int, C.c_int, F, F, P, P], C.c_int),
+    "fno_fold_drbig": ([C.c_int, C.c_int, F, F, F, P], C.c_int),
+    "fno_gelu_fwd": ([C.c_longlong, F, P, P, P], C.c_int),
+    "fno_gelu_bwd": ([C.c_longlong, P, F, P, P, P], C.c_int),
+    "fno_meanpool": ([C.c_int, C.c_int, C.c_int, P, P, P], C.c_int),
+    "fno_meanpool_bwd": ([C.c_int, C.c_int, C.c_int, F, P, P], C.c_int),
+    "fno_colsum": ([C.c_longlong, C.c_int, P, F, F, P], C.c_int),
+    "fno_sum_parts": ([C.c_int, C.c_longlong, F, F, P], C.c_int),
+    "fno_mse": ([C.c_int, C.c_int, F, F, F, F, P], C.c_int),
+    "fno_adam": ([C.c_longlong, F, F, F, F, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, P, P], C.c_int),
+    "fno_to_bf16": ([C.c_longlong, F, P, P], C.c_int),
     "fdtd1d_batch_plan": ([P, C.c_int, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_int)], C.c_int),
     "fdtd1d_batch_run": ([C.POINTER(BatchParams1D), C.POINTER(BatchOut1D), P, C.c_int, C.c_int, C.c_int, C.c_int,
                           C.c_int, C.c_longlong, P], C.c_int),

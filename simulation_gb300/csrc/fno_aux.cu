@@ -1,0 +1,328 @@
+// Element-wise and reduction kernels of the 1D Fourier-neural-operator
+// surrogate (the GEMMs run in gemm_tc.cu): lift, mode permutes between the
+// DFT layout [B][C][2M] and the mode-major mixing layout [M][B][2C], complex
+// weight expansion, GELU backward, mean pooling, column sums, per-sample
+// partial sums, MSE loss and Adam.  No reference counterpart.
+#include <cuda_bf16.h>
+
+#include "fdtd_common.cuh"
+
+namespace fdtd {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+  // d/dz [z * Phi(z)] = Phi(z) + z * phi(z)
+  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+  const float pdf = 0.3989422804014327f * expf(-0.5f * z * z);
+  return cdf + z * pdf;
+}
+
+inline dim3 grid1(size_t n, int t = 256) {
+  size_t b = (n + t - 1) / t;
+  if (b > 152 * 64) b = 152 * 64;
+  return dim3((unsigned)b);
+}
+
+// x0[r][c] = gelu? no: x0 = P[c][0]*in[r][0] + P[c][1]*in[r][1] + p[c]   (r = b*N + n)
+__global__ void k_lift_fwd(size_t rows, int C, const float* __restrict__ in, const float* __restrict__ P,
+                           const float* __restrict__ p, bf16* __restrict__ x0) {
+  const size_t total = rows * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = i / C;
+    const int c = (int)(i % C);
+    const float v = fmaf(P[2 * c], in[2 * r], fmaf(P[2 * c + 1], in[2 * r + 1], p[c]));
+    x0[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// dP[c][j] += sum_r dx0[r][c]*in[r][j]; dp[c] += sum_r dx0[r][c]   (block per channel group)
+__global__ void k_lift_bwd(size_t rows, int C, const float* __restrict__ in, const bf16* __restrict__ dx0,
+                           float* __restrict__ dP, float* __restrict__ dp) {
+  const int c = blockIdx.y;
+  float s0 = 0.f, s1 = 0.f, sb = 0.f;
+  for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < rows; r += (size_t)gridDim.x * blockDim.x) {
+    const float d = __bfloat162float(dx0[r * C + c]);
+    s0 = fmaf(d, in[2 * r], s0);
+    s1 = fmaf(d, in[2 * r + 1], s1);
+    sb += d;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    sb += __shfl_down_sync(0xffffffffu, sb, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&dP[2 * c], s0);
+    atomicAdd(&dP[2 * c + 1], s1);
+    atomicAdd(&dp[c], sb);
+  }
+}
+
+// DFT layout [B][C][2M] (cos rows 0..M-1, -sin rows M..2M-1) -> mode-major
+// [M][B][2C] with [Re | Im] along the last axis; and the inverse permute
+__global__ void k_dft_to_modes(int B, int C, int M, const float* __restrict__ F, bf16* __restrict__ Fm) {
+  const size_t total = (size_t)B * C * 2 * M;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i % (2 * M));
+    const size_t bc = i / (2 * M);
+    const int c = (int)(bc % C);
+    const int b = (int)(bc / C);
+    const int k = j < M ? j : j - M;
+    const int part = j < M ? 0 : 1;
+    Fm[((size_t)k * B + b) * 2 * C + part * C + c] = __float2bfloat16_rn(F[i]);
+  }
+}
+
+__global__ void k_modes_to_dft(int B, int C, int M, const float* __restrict__ Gm, bf16* __restrict__ G) {
+  const size_t total = (size_t)B * C * 2 * M;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(i % (2 * M));
+    const size_t bc = i / (2 * M);
+    const int c = (int)(bc % C);
+    const int b = (int)(bc / C);
+    const int k = j < M ? j : j - M;
+    const int part = j < M ? 0 : 1;
+    G[i] = __float2bfloat16_rn(Gm[((size_t)k * B + b) * 2 * C + part * C + c]);
+  }
+}
+
+// complex per-mode weights R = Rr + i Ri acting on [Re|Im]: Rbig = [[Rr, -Ri], [Ri, Rr]]
+__global__ void k_build_rbig(int M, int C, const float* __restrict__ Rr, const float* __restrict__ Ri,
+                             bf16* __restrict__ Rbig) {
+  const size_t total = (size_t)M * 4 * C * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int col = (int)(i % (2 * C));
+    const int row = (int)((i / (2 * C)) % (2 * C));
+    const int k = (int)(i / (4 * (size_t)C * C));
+    const int ro = row % C, co = col % C;
+    const size_t s = ((size_t)k * C + ro) * C + co;
+    float v;
+    if (row < C) v = (col < C) ? Rr[s] : -Ri[s];
+    else v = (col < C) ? Ri[s] : Rr[s];
+    Rbig[i] = __float2bfloat16_rn(v);
+  }
+}
+
+__global__ void k_fold_drbig(int M, int C, const float* __restrict__ dRbig, float* __restrict__ dRr,
+                             float* __restrict__ dRi) {
+  const size_t total = (size_t)M * C * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int co = (int)(i % C);
+    const int ro = (int)((i / C) % C);
+    const int k = (int)(i / ((size_t)C * C));
+    const size_t b = (size_t)k * 4 * C * C;
+    const size_t w = 2 * (size_t)C;
+    const float a00 = dRbig[b + ro * w + co], a01 = dRbig[b + ro * w + C + co];
+    const float a10 = dRbig[b + (C + ro) * w + co], a11 = dRbig[b + (C + ro) * w + C + co];
+    dRr[i] += a00 + a11;
+    dRi[i] += a10 - a01;
+  }
+}
+
+// dz = dy * gelu'(z)   (z = stored pre-activation, BF16)
+__global__ void k_gelu_bwd(size_t n, const bf16* __restrict__ dy16, const float* __restrict__ dy32,
+                           const bf16* __restrict__ pre, bf16* __restrict__ dz) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float d = dy16 ? __bfloat162float(dy16[i]) : dy32[i];
+    dz[i] = __float2bfloat16_rn(d * gelu_grad(__bfloat162float(pre[i])));
+  }
+}
+
+// h[b][c] = mean_n x[b][n][c]
+__global__ void k_meanpool(int B, int N, int C, const bf16* __restrict__ x, bf16* __restrict__ h) {
+  const int b = blockIdx.x;
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    float s = 0.f;
+    for (int n = 0; n < N; ++n) s += __bfloat162float(x[((size_t)b * N + n) * C + c]);
+    h[(size_t)b * C + c] = __float2bfloat16_rn(s / N);
+  }
+}
+
+// dx[b][n][c] = dh[b][c] / N
+__global__ void k_meanpool_bwd(int B, int N, int C, const float* __restrict__ dh, bf16* __restrict__ dx) {
+  const size_t total = (size_t)B * N * C;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % C);
+    const int b = (int)(i / ((size_t)N * C));
+    dx[i] = __float2bfloat16_rn(dh[(size_t)b * C + c] / N);
+  }
+}
+
+// out[c] += sum_r x[r][c]   (BF16 or FP32 input)
+__global__ void k_colsum(size_t rows, int C, const bf16* __restrict__ x16, const float* __restrict__ x32,
+                         float* __restrict__ out) {
+  const int c = blockIdx.y * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  float s = 0.f;
+  for (size_t r = blockIdx.x; r < rows; r += gridDim.x)
+    s += x16 ? __bfloat162float(x16[r * C + c]) : x32[r * C + c];
+  atomicAdd(&out[c], s);
+}
+
+// out[i] += sum_b parts[b][i]
+__global__ void k_sum_parts(int nb, size_t n, const float* __restrict__ parts, float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int b = 0; b < nb; ++b) s += parts[(size_t)b * n + i];
+    out[i] += s;
+  }
+}
+
+// loss = sum (o - y)^2 / (B * D); dO = 2 (o - y) / (B * D)
+__global__ void k_mse(int B, int D, const float* __restrict__ o, const float* __restrict__ y, float* __restrict__ dO,
+                      float* __restrict__ loss) {
+  const size_t n = (size_t)B * D;
+  const float inv = 1.0f / (float)n;
+  float s = 0.f;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float d = o[i] - y[i];
+    dO[i] = 2.0f * d * inv;
+    s += d * d * inv;
+  }
+  for (int k = 16; k > 0; k >>= 1) s += __shfl_down_sync(0xffffffffu, s, k);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, s);
+}
+
+// Adam (Kingma & Ba 2015) on FP32 master weights; writes a BF16 copy if given
+__global__ void k_adam(size_t n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1, float bc2,
+                       bf16* __restrict__ w16) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+    w[i] = wi;
+    if (w16) w16[i] = __float2bfloat16_rn(wi);
+  }
+}
+
+__global__ void k_to_bf16(size_t n, const float* __restrict__ x, bf16* __restrict__ y) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    y[i] = __float2bfloat16_rn(x[i]);
+}
+
+__global__ void k_gelu_fwd(size_t n, const float* __restrict__ z, bf16* __restrict__ y, bf16* __restrict__ pre) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if (pre) pre[i] = __float2bfloat16_rn(z[i]);
+    y[i] = __float2bfloat16_rn(gelu_f(z[i]));
+  }
+}
+
+}  // namespace
+}  // namespace fdtd
+
+// ======================================================================= C-ABI
+// One entry point per surrogate helper; sizes are validated, pointers are
+// device pointers, nothing synchronises the host.
+using fdtd::bf16;
+#define FNO_LAUNCH(kern, grid, block, ...)                       \
+  do {                                                           \
+    kern<<<grid, block, 0, (cudaStream_t)stream>>>(__VA_ARGS__); \
+    return fdtd_host::check_launch();                            \
+  } while (0)
+
+extern "C" {
+
+int fno_lift_fwd(long long rows, int C, const float* in, const float* P, const float* p, void* x0,
+                 fdtd_stream_t stream) {
+  if (!in || !P || !p || !x0) return FDTD_ERR_NULL;
+  if (rows < 1 || C < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_lift_fwd, fdtd::grid1((size_t)rows * C), 256, (size_t)rows, C, in, P, p, (bf16*)x0);
+}
+
+int fno_lift_bwd(long long rows, int C, const float* in, const void* dx0, float* dP, float* dp,
+                 fdtd_stream_t stream) {
+  if (!in || !dx0 || !dP || !dp) return FDTD_ERR_NULL;
+  if (rows < 1 || C < 1 || C > 65535) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_lift_bwd, dim3(64, C), 256, (size_t)rows, C, in, (const bf16*)dx0, dP, dp);
+}
+
+int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_t stream) {
+  if (!F || !Fm) return FDTD_ERR_NULL;
+  if (B < 1 || C < 1 || M < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_dft_to_modes, fdtd::grid1((size_t)B * C * 2 * M), 256, B, C, M, F, (bf16*)Fm);
+}
+
+int fno_modes_to_dft(int B, int C, int M, const float* Gm, void* G, fdtd_stream_t stream) {
+  if (!Gm || !G) return FDTD_ERR_NULL;
+  if (B < 1 || C < 1 || M < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_modes_to_dft, fdtd::grid1((size_t)B * C * 2 * M), 256, B, C, M, Gm, (bf16*)G);
+}
+
+int fno_build_rbig(int M, int C, const float* Rr, const float* Ri, void* Rbig, fdtd_stream_t stream) {
+  if (!Rr || !Ri || !Rbig) return FDTD_ERR_NULL;
+  if (M < 1 || C < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_build_rbig, fdtd::grid1((size_t)M * 4 * C * C), 256, M, C, Rr, Ri, (bf16*)Rbig);
+}
+
+int fno_fold_drbig(int M, int C, const float* dRbig, float* dRr, float* dRi, fdtd_stream_t stream) {
+  if (!dRbig || !dRr || !dRi) return FDTD_ERR_NULL;
+  if (M < 1 || C < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_fold_drbig, fdtd::grid1((size_t)M * C * C), 256, M, C, dRbig, dRr, dRi);
+}
+
+int fno_gelu_bwd(long long n, const void* dy16, const float* dy32, const void* pre, void* dz, fdtd_stream_t stream) {
+  if ((!dy16 && !dy32) || !pre || !dz) return FDTD_ERR_NULL;
+  if (n < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_gelu_bwd, fdtd::grid1((size_t)n), 256, (size_t)n, (const bf16*)dy16, dy32, (const bf16*)pre,
+             (bf16*)dz);
+}
+
+int fno_gelu_fwd(long long n, const float* z, void* y, void* pre, fdtd_stream_t stream) {
+  if (!z || !y) return FDTD_ERR_NULL;
+  if (n < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_gelu_fwd, fdtd::grid1((size_t)n), 256, (size_t)n, z, (bf16*)y, (bf16*)pre);
+}
+
+int fno_meanpool(int B, int N, int C, const void* x, void* h, fdtd_stream_t stream) {
+  if (!x || !h) return FDTD_ERR_NULL;
+  if (B < 1 || N < 1 || C < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_meanpool, dim3(B), 128, B, N, C, (const bf16*)x, (bf16*)h);
+}
+
+int fno_meanpool_bwd(int B, int N, int C, const float* dh, void* dx, fdtd_stream_t stream) {
+  if (!dh || !dx) return FDTD_ERR_NULL;
+  if (B < 1 || N < 1 || C < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_meanpool_bwd, fdtd::grid1((size_t)B * N * C), 256, B, N, C, dh, (bf16*)dx);
+}
+
+int fno_colsum(long long rows, int C, const void* x16, const float* x32, float* out, fdtd_stream_t stream) {
+  if ((!x16 && !x32) || !out) return FDTD_ERR_NULL;
+  if (rows < 1 || C < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_colsum, dim3(256, (C + 127) / 128), 128, (size_t)rows, C, (const bf16*)x16, x32, out);
+}
+
+int fno_sum_parts(int nb, long long n, const float* parts, float* out, fdtd_stream_t stream) {
+  if (!parts || !out) return FDTD_ERR_NULL;
+  if (nb < 1 || n < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_sum_parts, fdtd::grid1((size_t)n), 256, nb, (size_t)n, parts, out);
+}
+
+int fno_mse(int B, int D, const float* o, const float* y, float* dO, float* loss, fdtd_stream_t stream) {
+  if (!o || !y || !dO || !loss) return FDTD_ERR_NULL;
+  if (B < 1 || D < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_mse, fdtd::grid1((size_t)B * D), 256, B, D, o, y, dO, loss);
+}
+
+int fno_adam(long long n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
+             int step, void* w16, fdtd_stream_t stream) {
+  if (!w || !g || !m || !v) return FDTD_ERR_NULL;
+  if (n < 1 || step < 1) return FDTD_ERR_SIZE;
+  const float bc1 = 1.f - powf(b1, (float)step), bc2 = 1.f - powf(b2, (float)step);
+  FNO_LAUNCH(fdtd::k_adam, fdtd::grid1((size_t)n), 256, (size_t)n, w, g, m, v, lr, b1, b2, eps, bc1, bc2,
+             (bf16*)w16);
+}
+
+int fno_to_bf16(long long n, const float* x, void* y, fdtd_stream_t stream) {
+  if (!x || !y) return FDTD_ERR_NULL;
+  if (n < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_to_bf16, fdtd::grid1((size_t)n), 256, (size_t)n, x, (bf16*)y);
+}
+
+}  // extern "C"

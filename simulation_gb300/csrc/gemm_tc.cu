@@ -1,0 +1,374 @@
+// BF16 tensor-core GEMM for sm_103a (tcgen05 + TMA + TMEM), FP32 accumulation,
+// with a fused epilogue (scale, bias, residual, GELU, accumulate, BF16/FP32
+// output).  Written for the neural-operator surrogate's contractions
+// (truncated DFT, inverse DFT, channel mixing, pointwise layers and their
+// gradients).
+//
+// One 128 x BN output tile per CTA of 4 warps:
+//   * warp 0, one lane: TMA producer.  Each pipeline stage holds a 128 x 64
+//     A tile and a BN x 64 B tile in 128-byte-swizzled shared memory, loaded
+//     by cp.async.bulk.tensor with mbarrier completion;
+//   * warp 1, one lane: issues tcgen05.mma (kind::f16, BF16 inputs, FP32
+//     accumulator in TMEM), four 16-deep MMAs per stage, and tcgen05.commit
+//     to release the stage and finally to signal the epilogue;
+//   * all four warps: read the accumulator with tcgen05.ld (warp w owns TMEM
+//     lanes 32w..32w+31 = output rows), apply the epilogue and store.
+// Operands may be K-major or MN-major (the transposed products of the
+// backward pass need MN-major), selected per call.  Every wait on an mbarrier
+// is bounded (about 2 s): on expiry the kernel records FDTD_STATUS_TIMEOUT in
+// the status word and finishes without further waits.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "fdtd_common.cuh"
+
+namespace fdtd {
+namespace {
+
+constexpr int BM = 128;
+constexpr int BK = 64;      // one 128-byte swizzle atom of BF16 along K
+constexpr int STAGES = 4;
+constexpr int THREADS = 128;
+
+struct GemmArgs {
+  int M, N, K, batch;
+  int a_mn, b_mn;
+  float* c32;
+  __nv_bfloat16* c16;
+  long long ldc, stride_c;
+  const float* bias;
+  const __nv_bfloat16* res16;
+  long long ldr, stride_r;
+  float alpha;
+  int act;
+  int accumulate;
+  __nv_bfloat16* pre16;  // optional pre-activation output (same layout as C)
+  unsigned lbo_mn, sbo_mn;
+  int a_shared, b_shared;  // operand shared by every batch entry (batch stride 0)
+  int* status;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes) : "memory");
+}
+
+// bounded wait on an mbarrier phase; false (and TIMEOUT recorded) on expiry
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, int* status) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > 4000000000LL) {
+      raise_status(status, ST_TIMEOUT);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2,
+                                            uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(mbar)
+      : "memory");
+}
+
+// shared-memory matrix descriptor (tcgen05): start address, leading and
+// stride byte offsets (16-byte units), descriptor version 1, 128B swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// instruction descriptor, kind::f16: BF16 A and B, FP32 accumulator, M x N
+__host__ __device__ constexpr uint32_t instr_desc(int m, int n, int a_mn, int b_mn) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)a_mn << 15) | ((uint32_t)b_mn << 16) |
+         ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+
+template <int BN>
+__global__ void __launch_bounds__(THREADS, 1)
+    k_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const GemmArgs a) {
+  constexpr uint32_t A_BYTES = BM * BK * 2;
+  constexpr uint32_t B_BYTES = BN * BK * 2;
+  constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1024-byte aligned tile area (128B swizzle atoms), then barriers
+  unsigned char* tiles = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + STAGES * STAGE_BYTES);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + STAGES;
+  uint64_t* done = bars + 2 * STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+
+  const int warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
+  const int n0 = blockIdx.x * BN;
+  const int m0 = blockIdx.y * BM;
+  const int bz = blockIdx.z;
+  const int kblocks = (a.K + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    mbar_init(smem_u32(done), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  bool ok = true;
+  if (warp == 0 && lane == 0) {
+    // ------------------------------------------------ producer
+    for (int kb = 0; kb < kblocks && ok; ++kb) {
+      const int s = kb % STAGES;
+      if (kb >= STAGES) ok = mbar_wait(smem_u32(&empty[s]), ((kb / STAGES) - 1) & 1, a.status);
+      if (!ok) break;
+      const uint32_t fb = smem_u32(&full[s]);
+      mbar_expect_tx(fb, STAGE_BYTES);
+      const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
+      const uint32_t sb = sa + A_BYTES;
+      const int k0 = kb * BK;
+      const int za = a.a_shared ? 0 : bz, zb = a.b_shared ? 0 : bz;
+      if (!a.a_mn) {
+        tma_load_3d(sa, &tmA, k0, m0, za, fb);
+      } else {
+        tma_load_3d(sa, &tmA, m0, k0, za, fb);
+        tma_load_3d(sa + A_BYTES / 2, &tmA, m0 + 64, k0, za, fb);
+      }
+      if (!a.b_mn) {
+        tma_load_3d(sb, &tmB, k0, n0, zb, fb);
+      } else {
+#pragma unroll
+        for (int h = 0; h < BN / 64; ++h) tma_load_3d(sb + h * (BK * 128), &tmB, n0 + 64 * h, k0, zb, fb);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ------------------------------------------------ MMA issuer
+    const uint32_t idesc = instr_desc(BM, BN, a.a_mn, a.b_mn);
+    for (int kb = 0; kb < kblocks && ok; ++kb) {
+      const int s = kb % STAGES;
+      ok = mbar_wait(smem_u32(&full[s]), (kb / STAGES) & 1, a.status);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
+      const uint32_t sb = sa + A_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk) {
+        // K-major: step 32 bytes inside the swizzle atom; MN-major: 16 K rows of 128 bytes
+        const uint64_t ad = a.a_mn ? smem_desc(sa + kk * 2048, a.lbo_mn, a.sbo_mn) : smem_desc(sa + kk * 32, 16, 1024);
+        const uint64_t bd = a.b_mn ? smem_desc(sb + kk * 2048, a.lbo_mn, a.sbo_mn) : smem_desc(sb + kk * 32, 16, 1024);
+        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      // the stage is free once these MMAs have read it
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&empty[s]))
+                   : "memory");
+    }
+    if (ok)
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(done))
+                   : "memory");
+  }
+  __syncwarp();
+
+  // ------------------------------------------------ epilogue (all warps)
+  const bool have = __all_sync(0xffffffffu, (kblocks > 0) && mbar_wait(smem_u32(done), 0, a.status));
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const int row = m0 + warp * 32 + lane;
+  const size_t cbase = (size_t)bz * a.stride_c + (size_t)row * a.ldc;
+  const size_t rbase = (size_t)bz * a.stride_r + (size_t)row * a.ldr;
+#pragma unroll 1
+  for (int c0 = 0; c0 < BN; c0 += 32) {
+    uint32_t r[32];
+    if (have) {
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    } else {
+#pragma unroll
+      for (int q = 0; q < 32; ++q) r[q] = 0u;
+    }
+    if (row < a.M) {
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int col = n0 + c0 + q;
+        if (col < a.N) {
+          float z = __fmul_rn(a.alpha, __uint_as_float(r[q]));
+          if (a.bias) z = __fadd_rn(z, a.bias[col]);
+          if (a.res16) z = __fadd_rn(z, __bfloat162float(a.res16[rbase + col]));
+          if (a.pre16) a.pre16[cbase + col] = __float2bfloat16_rn(z);
+          float y = a.act == 1 ? gelu(z) : z;
+          if (a.c32) {
+            if (a.accumulate) y = __fadd_rn(y, a.c32[cbase + col]);
+            a.c32[cbase + col] = y;
+          } else {
+            if (a.accumulate) y = __fadd_rn(y, __bfloat162float(a.c16[cbase + col]));
+            a.c16[cbase + col] = __float2bfloat16_rn(y);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  }
+}
+
+// ----------------------------------------------------------------- host
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::mutex g_encode_mu;
+
+int get_encode() {
+  std::lock_guard<std::mutex> lk(g_encode_mu);
+  if (g_encode) return FDTD_OK;
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn) {
+    fdtd_host::note_cuda_error(e);
+    return FDTD_ERR_CUDA;
+  }
+  g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  return FDTD_OK;
+}
+
+// 3D tensor map over a BF16 operand: dims {inner, outer, batch}
+int make_map(CUtensorMap* tm, const void* base, uint64_t inner, uint64_t outer, uint64_t batch, uint64_t ld_elems,
+             uint64_t stride_elems, uint32_t box_inner, uint32_t box_outer) {
+  cuuint64_t dims[3] = {inner, outer, batch};
+  cuuint64_t strides[2] = {ld_elems * 2, stride_elems * 2};
+  cuuint32_t box[3] = {box_inner, box_outer, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  const CUresult r = g_encode(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
+                              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? FDTD_OK : FDTD_ERR_ARG;
+}
+
+template <int BN>
+size_t smem_bytes() {
+  return 1024 + (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * STAGES + 2) + 32768;  // + guard
+}
+
+template <int BN>
+int launch_gemm_t(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g, cudaStream_t st) {
+  auto kern = k_gemm<BN>;
+  const size_t smem = smem_bytes<BN>();
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    fdtd_host::note_cuda_error(e);
+    return FDTD_ERR_CUDA;
+  }
+  const dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.batch);
+  kern<<<grid, THREADS, smem, st>>>(ta, tb, g);
+  return fdtd_host::check_launch();
+}
+
+}  // namespace
+}  // namespace fdtd
+
+extern "C" int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_t stream) {
+  using namespace fdtd;
+  if (!d || !d->A || !d->B) return FDTD_ERR_NULL;
+  if (!d->C32 == !d->C16) return FDTD_ERR_ARG;  // exactly one output
+  if (d->M < 1 || d->N < 1 || d->K < 1 || d->batch < 1) return FDTD_ERR_SIZE;
+  if (d->N > 65535 * 128 || d->M > 65535 * BM || d->batch > 65535) return FDTD_ERR_SIZE;
+  auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+  if (!al16(d->A) || !al16(d->B)) return FDTD_ERR_ALIGN;
+  if (d->lda % 8 || d->ldb % 8 || (d->batch > 1 && (d->stride_a % 8 || d->stride_b % 8))) return FDTD_ERR_ALIGN;
+  if (d->act < 0 || d->act > 1) return FDTD_ERR_ARG;
+  if ((d->a_mn_major ? d->lda < d->M : d->lda < d->K) || (d->b_mn_major ? d->ldb < d->N : d->ldb < d->K))
+    return FDTD_ERR_SIZE;
+  int rc = get_encode();
+  if (rc) return rc;
+  const int BN = (d->N <= 64) ? 64 : 128;
+  CUtensorMap ta, tb;
+  // an operand with batch stride 0 is shared: one batch slice in its map
+  const bool a_sh = d->batch == 1 || d->stride_a == 0;
+  const bool b_sh = d->batch == 1 || d->stride_b == 0;
+  const uint64_t sa = a_sh ? (uint64_t)d->lda * (d->a_mn_major ? d->K : d->M) : (uint64_t)d->stride_a;
+  const uint64_t sb = b_sh ? (uint64_t)d->ldb * (d->b_mn_major ? d->K : d->N) : (uint64_t)d->stride_b;
+  const uint64_t ba = a_sh ? 1 : (uint64_t)d->batch, bb = b_sh ? 1 : (uint64_t)d->batch;
+  if (!d->a_mn_major) rc = make_map(&ta, d->A, d->K, d->M, ba, d->lda, sa, BK, BM);
+  else rc = make_map(&ta, d->A, d->M, d->K, ba, d->lda, sa, 64, BK);
+  if (rc) return rc;
+  if (!d->b_mn_major) rc = make_map(&tb, d->B, d->K, d->N, bb, d->ldb, sb, BK, BN);
+  else rc = make_map(&tb, d->B, d->N, d->K, bb, d->ldb, sb, 64, BK);
+  if (rc) return rc;
+  GemmArgs g{};
+  g.M = d->M;
+  g.N = d->N;
+  g.K = d->K;
+  g.batch = d->batch;
+  g.a_mn = d->a_mn_major;
+  g.b_mn = d->b_mn_major;
+  g.c32 = d->C32;
+  g.c16 = reinterpret_cast<__nv_bfloat16*>(d->C16);
+  g.ldc = d->ldc;
+  g.stride_c = d->stride_c;
+  g.bias = d->bias;
+  g.res16 = reinterpret_cast<const __nv_bfloat16*>(d->res16);
+  g.ldr = d->ldr;
+  g.stride_r = d->stride_r;
+  g.alpha = d->alpha;
+  g.act = d->act;
+  g.accumulate = d->accumulate;
+  g.pre16 = reinterpret_cast<__nv_bfloat16*>(d->pre16);
+  g.lbo_mn = d->mn_lbo ? (unsigned)d->mn_lbo : (unsigned)(BK * 128);
+  g.sbo_mn = d->mn_sbo ? (unsigned)d->mn_sbo : 1024u;
+  g.a_shared = a_sh ? 1 : 0;
+  g.b_shared = b_sh ? 1 : 0;
+  g.status = status;
+  if (BN == 64) return launch_gemm_t<64>(ta, tb, g, (cudaStream_t)stream);
+  return launch_gemm_t<128>(ta, tb, g, (cudaStream_t)stream);
+}

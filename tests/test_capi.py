@@ -20,7 +20,8 @@ def lib():
 def _declared():
     src = open(os.path.join(ROOT, "include", "fdtd.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\**\s+\**(fdtd[a-z0-9_]*)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\**\s+\**((?:fdtd|fno)[a-z0-9_]*)\s*\(", src,
+                                 flags=re.M)))
 
 
 def test_exports_every_declared_symbol(lib):
