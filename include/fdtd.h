@@ -235,10 +235,19 @@ typedef struct {
   const void* res16;
   long long ldr, stride_r;
   float alpha;
-  int act; /* 0 none, 1 GELU (erf form) */
+  int act; /* 0 none, 1 GELU (tanh form) */
   int accumulate;
   void* pre16;
   int mn_lbo, mn_sbo; /* descriptor byte offsets for MN-major tiles (0 = default) */
+  /* optional second product accumulated into the same tile before the
+   * epilogue: acc = A.B' + A2.B2' (same M, N; its own K2, layouts, strides) */
+  int K2;
+  const void* A2;
+  long long lda2, stride_a2;
+  int a2_mn_major;
+  const void* B2;
+  long long ldb2, stride_b2;
+  int b2_mn_major;
 } fdtd_gemm_desc;
 
 int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_t stream);
@@ -263,6 +272,9 @@ int fno_meanpool_bwd(int B, int N, int C, const float* dh, void* dx, fdtd_stream
 int fno_colsum(long long rows, int C, const void* x16, const float* x32, float* out, fdtd_stream_t stream);
 int fno_sum_parts(int nb, long long n, const float* parts, float* out, fdtd_stream_t stream);
 int fno_mse(int B, int D, const float* o, const float* y, float* dO, float* loss, fdtd_stream_t stream);
+/* relative squared error per sample, ||o-y||^2 / max(||y||^2, floor2), averaged over the batch */
+int fno_rel_mse(int B, int D, float floor2, const float* o, const float* y, float* dO, float* loss,
+                fdtd_stream_t stream);
 int fno_adam(long long n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
              int step, void* w16, fdtd_stream_t stream);
 int fno_to_bf16(long long n, const float* x, void* y, fdtd_stream_t stream);

@@ -22,7 +22,8 @@ def dft_matrices(n: int, m: int):
 
 
 def gelu(z):
-    return 0.5 * z * (1.0 + torch.erf(z / np.sqrt(2.0)))
+    """GELU, tanh form (Hendrycks & Gimpel 2016), as the GPU kernels use it."""
+    return 0.5 * z * (1.0 + torch.tanh(np.sqrt(2.0 / np.pi) * (z + 0.044715 * z ** 3)))
 
 
 def forward(params: dict, inp: torch.Tensor, layers: int, modes: int) -> torch.Tensor:

@@ -79,7 +79,9 @@ class GemmDesc(C.Structure):
                 ("C32", P), ("C16", P), ("ldc", C.c_longlong), ("stride_c", C.c_longlong),
                 ("bias", P), ("res16", P), ("ldr", C.c_longlong), ("stride_r", C.c_longlong),
                 ("alpha", C.c_float), ("act", C.c_int), ("accumulate", C.c_int), ("pre16", P),
-                ("mn_lbo", C.c_int), ("mn_sbo", C.c_int)]
+                ("mn_lbo", C.c_int), ("mn_sbo", C.c_int),
+                ("K2", C.c_int), ("A2", P), ("lda2", C.c_longlong), ("stride_a2", C.c_longlong), ("a2_mn_major", C.c_int),
+                ("B2", P), ("ldb2", C.c_longlong), ("stride_b2", C.c_longlong), ("b2_mn_major", C.c_int)]
 
 
 class Params1D(C.Structure):
@@ -148,6 +150,7 @@ _SIGS = {
     "fno_colsum": ([C.c_longlong, C.c_int, P, F, F, P], C.c_int),
     "fno_sum_parts": ([C.c_int, C.c_longlong, F, F, P], C.c_int),
     "fno_mse": ([C.c_int, C.c_int, F, F, F, F, P], C.c_int),
+    "fno_rel_mse": ([C.c_int, C.c_int, C.c_float, F, F, F, F, P], C.c_int),
     "fno_adam": ([C.c_longlong, F, F, F, F, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int, P, P], C.c_int),
     "fno_to_bf16": ([C.c_longlong, F, P, P], C.c_int),
     "fdtd1d_batch_plan": ([P, C.c_int, C.c_int, C.c_int, P, C.c_size_t, C.POINTER(C.c_int)], C.c_int),

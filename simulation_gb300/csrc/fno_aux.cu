@@ -12,12 +12,22 @@ namespace {
 
 using bf16 = __nv_bfloat16;
 
-__device__ __forceinline__ float gelu_f(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU, tanh form (Hendrycks & Gimpel 2016), the same function as the GEMM
+// epilogue: 0.5 z (1 + tanh(u)), u = sqrt(2/pi) (z + 0.044715 z^3)
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu_f(float z) {
+  const float u = 0.7978845608028654f * fmaf(0.044715f * z, z * z, z);
+  return 0.5f * z * (1.0f + tanh_hw(u));
+}
 __device__ __forceinline__ float gelu_grad(float z) {
-  // d/dz [z * Phi(z)] = Phi(z) + z * phi(z)
-  const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
-  const float pdf = 0.3989422804014327f * expf(-0.5f * z * z);
-  return cdf + z * pdf;
+  // d/dz = 0.5 (1 + t) + 0.5 z (1 - t^2) sqrt(2/pi) (1 + 3*0.044715 z^2)
+  const float u = 0.7978845608028654f * fmaf(0.044715f * z, z * z, z);
+  const float t = tanh_hw(u);
+  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * fmaf(0.134145f * z, z, 1.0f);
 }
 
 inline dim3 grid1(size_t n, int t = 256) {
@@ -26,7 +36,7 @@ inline dim3 grid1(size_t n, int t = 256) {
   return dim3((unsigned)b);
 }
 
-// x0[r][c] = gelu? no: x0 = P[c][0]*in[r][0] + P[c][1]*in[r][1] + p[c]   (r = b*N + n)
+// lift: x0[r][c] = P[c][0]*in[r][0] + P[c][1]*in[r][1] + p[c]   (r = b*N + n)
 __global__ void k_lift_fwd(size_t rows, int C, const float* __restrict__ in, const float* __restrict__ P,
                            const float* __restrict__ p, bf16* __restrict__ x0) {
   const size_t total = rows * C;
@@ -186,6 +196,43 @@ __global__ void k_mse(int B, int D, const float* __restrict__ o, const float* __
   if ((threadIdx.x & 31) == 0) atomicAdd(loss, s);
 }
 
+// relative loss per sample: w_b = 1 / max(||y_b||^2, floor2);
+// loss = mean_b w_b ||o_b - y_b||^2, dO = 2 w_b (o_b - y_b) / B   (one block per sample)
+__global__ void k_rel_mse(int B, int D, float floor2, const float* __restrict__ o, const float* __restrict__ y,
+                          float* __restrict__ dO, float* __restrict__ loss) {
+  const int b = blockIdx.x;
+  __shared__ float red[2][32];
+  float sy = 0.f, sd = 0.f;
+  for (int d = threadIdx.x; d < D; d += blockDim.x) {
+    const float yy = y[(size_t)b * D + d], dd = o[(size_t)b * D + d] - yy;
+    sy += yy * yy;
+    sd += dd * dd;
+  }
+  for (int k = 16; k > 0; k >>= 1) {
+    sy += __shfl_down_sync(0xffffffffu, sy, k);
+    sd += __shfl_down_sync(0xffffffffu, sd, k);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) {
+    red[0][w] = sy;
+    red[1][w] = sd;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float ty = 0.f, td = 0.f;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+      ty += red[0][k];
+      td += red[1][k];
+    }
+    red[0][0] = 1.0f / fmaxf(ty, floor2);
+    atomicAdd(loss, td * red[0][0] / B);
+  }
+  __syncthreads();
+  const float wb = red[0][0];
+  for (int d = threadIdx.x; d < D; d += blockDim.x)
+    dO[(size_t)b * D + d] = 2.0f * wb * (o[(size_t)b * D + d] - y[(size_t)b * D + d]) / B;
+}
+
 // Adam (Kingma & Ba 2015) on FP32 master weights; writes a BF16 copy if given
 __global__ void k_adam(size_t n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, float lr, float b1, float b2, float eps, float bc1, float bc2,
@@ -308,6 +355,13 @@ int fno_mse(int B, int D, const float* o, const float* y, float* dO, float* loss
   if (!o || !y || !dO || !loss) return FDTD_ERR_NULL;
   if (B < 1 || D < 1) return FDTD_ERR_SIZE;
   FNO_LAUNCH(fdtd::k_mse, fdtd::grid1((size_t)B * D), 256, B, D, o, y, dO, loss);
+}
+
+int fno_rel_mse(int B, int D, float floor2, const float* o, const float* y, float* dO, float* loss,
+                fdtd_stream_t stream) {
+  if (!o || !y || !dO || !loss) return FDTD_ERR_NULL;
+  if (B < 1 || D < 1 || !(floor2 > 0)) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_rel_mse, dim3(B), 128, B, D, floor2, o, y, dO, loss);
 }
 
 int fno_adam(long long n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,

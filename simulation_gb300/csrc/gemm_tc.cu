@@ -4,15 +4,17 @@
 // (truncated DFT, inverse DFT, channel mixing, pointwise layers and their
 // gradients).
 //
-// One 128 x BN output tile per CTA of 4 warps:
-//   * warp 0, one lane: TMA producer.  Each pipeline stage holds a 128 x 64
+// 128 x BN output tiles, persistent CTAs of 6 warps:
+//   * warp 4, one lane: TMA producer.  Each pipeline stage holds a 128 x 64
 //     A tile and a BN x 64 B tile in 128-byte-swizzled shared memory, loaded
 //     by cp.async.bulk.tensor with mbarrier completion;
-//   * warp 1, one lane: issues tcgen05.mma (kind::f16, BF16 inputs, FP32
+//   * warp 5, one lane: issues tcgen05.mma (kind::f16, BF16 inputs, FP32
 //     accumulator in TMEM), four 16-deep MMAs per stage, and tcgen05.commit
-//     to release the stage and finally to signal the epilogue;
-//   * all four warps: read the accumulator with tcgen05.ld (warp w owns TMEM
-//     lanes 32w..32w+31 = output rows), apply the epilogue and store.
+//     to release the stage and, per tile, to signal the epilogue;
+//   * warps 0-3: read the accumulator with tcgen05.ld (warp w owns TMEM lanes
+//     32w..32w+31 = output rows), return the TMEM buffer, apply the epilogue
+//     and store; two accumulator buffers overlap a tile's epilogue with the
+//     next tile's MMAs.
 // Operands may be K-major or MN-major (the transposed products of the
 // backward pass need MN-major), selected per call.  Every wait on an mbarrier
 // is bounded (about 2 s): on expiry the kernel records FDTD_STATUS_TIMEOUT in
@@ -21,6 +23,7 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "fdtd_common.cuh"
@@ -30,8 +33,8 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BK = 64;      // one 128-byte swizzle atom of BF16 along K
-constexpr int STAGES = 4;
-constexpr int THREADS = 128;
+constexpr int EPI_WARPS = 4;
+constexpr int THREADS = 32 * (EPI_WARPS + 2);
 
 struct GemmArgs {
   int M, N, K, batch;
@@ -48,6 +51,10 @@ struct GemmArgs {
   __nv_bfloat16* pre16;  // optional pre-activation output (same layout as C)
   unsigned lbo_mn, sbo_mn;
   int a_shared, b_shared;  // operand shared by every batch entry (batch stride 0)
+  int vec_ok;              // epilogue pointers/strides allow 16-byte vector access
+  // optional second operand pair accumulated into the same tile: D += A2.B2'
+  int K2;
+  int a2_mn, b2_mn, a2_shared, b2_shared;
   int* status;
 };
 
@@ -108,41 +115,61 @@ __host__ __device__ constexpr uint32_t instr_desc(int m, int n, int a_mn, int b_
          ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU, tanh form (Hendrycks & Gimpel 2016): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3)))
+// with the hardware tanh approximation
+__device__ __forceinline__ float tanh_hw(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu(float z) {
+  const float u = 0.7978845608028654f * fmaf(0.044715f * z, z * z, z);
+  return 0.5f * z * (1.0f + tanh_hw(u));
+}
 
-template <int BN>
+// Persistent, warp-specialised kernel: warps 0-3 drain accumulators
+// (epilogue), warp 4 is the TMA producer, warp 5 issues the MMAs.  Two TMEM
+// accumulator buffers let the epilogue of one tile overlap the MMAs of the
+// next; tiles are taken round-robin (tile = blockIdx.x + i * gridDim.x, M tiles
+// fastest so neighbouring CTAs share B tiles in L2).
+template <int BN, int STAGES>
 __global__ void __launch_bounds__(THREADS, 1)
-    k_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const GemmArgs a) {
+    k_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+           const __grid_constant__ CUtensorMap tmA2, const __grid_constant__ CUtensorMap tmB2, const GemmArgs a) {
   constexpr uint32_t A_BYTES = BM * BK * 2;
   constexpr uint32_t B_BYTES = BN * BK * 2;
   constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // 1024-byte aligned tile area (128B swizzle atoms), then barriers
   unsigned char* tiles = reinterpret_cast<unsigned char*>(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + STAGES * STAGE_BYTES);
   uint64_t* full = bars;
   uint64_t* empty = bars + STAGES;
-  uint64_t* done = bars + 2 * STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+  uint64_t* tfull = bars + 2 * STAGES;
+  uint64_t* tempty = bars + 2 * STAGES + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 4);
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
-  const int n0 = blockIdx.x * BN;
-  const int m0 = blockIdx.y * BM;
-  const int bz = blockIdx.z;
-  const int kblocks = (a.K + BK - 1) / BK;
+  const int kb1 = (a.K + BK - 1) / BK;                       // k-blocks of the first pair
+  const int kblocks = kb1 + (a.K2 > 0 ? (a.K2 + BK - 1) / BK : 0);
+  const int mt = (a.M + BM - 1) / BM;
+  const int nt = (a.N + BN - 1) / BN;
+  const long long total = (long long)mt * nt * a.batch;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(smem_u32(&full[s]), 1);
       mbar_init(smem_u32(&empty[s]), 1);
     }
-    mbar_init(smem_u32(done), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&tfull[b]), 1);
+      mbar_init(smem_u32(&tempty[b]), EPI_WARPS);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(BN)
+                 "r"(2 * BN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -151,116 +178,222 @@ __global__ void __launch_bounds__(THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  bool ok = true;
-  if (warp == 0 && lane == 0) {
+  if (warp == EPI_WARPS) {
     // ------------------------------------------------ producer
-    for (int kb = 0; kb < kblocks && ok; ++kb) {
-      const int s = kb % STAGES;
-      if (kb >= STAGES) ok = mbar_wait(smem_u32(&empty[s]), ((kb / STAGES) - 1) & 1, a.status);
-      if (!ok) break;
-      const uint32_t fb = smem_u32(&full[s]);
-      mbar_expect_tx(fb, STAGE_BYTES);
-      const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
-      const uint32_t sb = sa + A_BYTES;
-      const int k0 = kb * BK;
-      const int za = a.a_shared ? 0 : bz, zb = a.b_shared ? 0 : bz;
-      if (!a.a_mn) {
-        tma_load_3d(sa, &tmA, k0, m0, za, fb);
-      } else {
-        tma_load_3d(sa, &tmA, m0, k0, za, fb);
-        tma_load_3d(sa + A_BYTES / 2, &tmA, m0 + 64, k0, za, fb);
-      }
-      if (!a.b_mn) {
-        tma_load_3d(sb, &tmB, k0, n0, zb, fb);
-      } else {
-#pragma unroll
-        for (int h = 0; h < BN / 64; ++h) tma_load_3d(sb + h * (BK * 128), &tmB, n0 + 64 * h, k0, zb, fb);
-      }
-    }
-  } else if (warp == 1 && lane == 0) {
-    // ------------------------------------------------ MMA issuer
-    const uint32_t idesc = instr_desc(BM, BN, a.a_mn, a.b_mn);
-    for (int kb = 0; kb < kblocks && ok; ++kb) {
-      const int s = kb % STAGES;
-      ok = mbar_wait(smem_u32(&full[s]), (kb / STAGES) & 1, a.status);
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
-      const uint32_t sb = sa + A_BYTES;
-#pragma unroll
-      for (int kk = 0; kk < BK / 16; ++kk) {
-        // K-major: step 32 bytes inside the swizzle atom; MN-major: 16 K rows of 128 bytes
-        const uint64_t ad = a.a_mn ? smem_desc(sa + kk * 2048, a.lbo_mn, a.sbo_mn) : smem_desc(sa + kk * 32, 16, 1024);
-        const uint64_t bd = a.b_mn ? smem_desc(sb + kk * 2048, a.lbo_mn, a.sbo_mn) : smem_desc(sb + kk * 32, 16, 1024);
-        const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-            : "memory");
-      }
-      // the stage is free once these MMAs have read it
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(&empty[s]))
-                   : "memory");
-    }
-    if (ok)
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(done))
-                   : "memory");
-  }
-  __syncwarp();
-
-  // ------------------------------------------------ epilogue (all warps)
-  const bool have = __all_sync(0xffffffffu, (kblocks > 0) && mbar_wait(smem_u32(done), 0, a.status));
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  const int row = m0 + warp * 32 + lane;
-  const size_t cbase = (size_t)bz * a.stride_c + (size_t)row * a.ldc;
-  const size_t rbase = (size_t)bz * a.stride_r + (size_t)row * a.ldr;
-#pragma unroll 1
-  for (int c0 = 0; c0 < BN; c0 += 32) {
-    uint32_t r[32];
-    if (have) {
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-            "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-            "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-          : "r"(taddr)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    } else {
-#pragma unroll
-      for (int q = 0; q < 32; ++q) r[q] = 0u;
-    }
-    if (row < a.M) {
-#pragma unroll
-      for (int q = 0; q < 32; ++q) {
-        const int col = n0 + c0 + q;
-        if (col < a.N) {
-          float z = __fmul_rn(a.alpha, __uint_as_float(r[q]));
-          if (a.bias) z = __fadd_rn(z, a.bias[col]);
-          if (a.res16) z = __fadd_rn(z, __bfloat162float(a.res16[rbase + col]));
-          if (a.pre16) a.pre16[cbase + col] = __float2bfloat16_rn(z);
-          float y = a.act == 1 ? gelu(z) : z;
-          if (a.c32) {
-            if (a.accumulate) y = __fadd_rn(y, a.c32[cbase + col]);
-            a.c32[cbase + col] = y;
+    if (lane == 0) {
+      long long g = 0;
+      bool ok = true;
+      for (long long t = blockIdx.x; t < total && ok; t += gridDim.x) {
+        const int bz = (int)(t / ((long long)mt * nt));
+        const int rem = (int)(t % ((long long)mt * nt));
+        const int m0 = (rem % mt) * BM, n0 = (rem / mt) * BN;
+        const int za = a.a_shared ? 0 : bz, zb = a.b_shared ? 0 : bz;
+        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+          const int s = (int)(g % STAGES);
+          if (g >= STAGES && !(ok = mbar_wait(smem_u32(&empty[s]), (uint32_t)(((g / STAGES) - 1) & 1), a.status)))
+            break;
+          const uint32_t fb = smem_u32(&full[s]);
+          mbar_expect_tx(fb, STAGE_BYTES);
+          const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
+          const uint32_t sb = sa + A_BYTES;
+          const bool second = kb >= kb1;
+          const CUtensorMap* ma = second ? &tmA2 : &tmA;
+          const CUtensorMap* mb = second ? &tmB2 : &tmB;
+          const int k0 = (second ? kb - kb1 : kb) * BK;
+          const int amn = second ? a.a2_mn : a.a_mn, bmn = second ? a.b2_mn : a.b_mn;
+          const int za2 = second ? (a.a2_shared ? 0 : bz) : za, zb2 = second ? (a.b2_shared ? 0 : bz) : zb;
+          if (!amn) {
+            tma_load_3d(sa, ma, k0, m0, za2, fb);
           } else {
-            if (a.accumulate) y = __fadd_rn(y, __bfloat162float(a.c16[cbase + col]));
-            a.c16[cbase + col] = __float2bfloat16_rn(y);
+            tma_load_3d(sa, ma, m0, k0, za2, fb);
+            tma_load_3d(sa + A_BYTES / 2, ma, m0 + 64, k0, za2, fb);
+          }
+          if (!bmn) {
+            tma_load_3d(sb, mb, k0, n0, zb2, fb);
+          } else {
+#pragma unroll
+            for (int h = 0; h < BN / 64; ++h) tma_load_3d(sb + h * (BK * 128), mb, n0 + 64 * h, k0, zb2, fb);
           }
         }
+      }
+    }
+  } else if (warp == EPI_WARPS + 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc1 = instr_desc(BM, BN, a.a_mn, a.b_mn);
+      const uint32_t idesc2 = instr_desc(BM, BN, a.a2_mn, a.b2_mn);
+      long long g = 0;
+      int i = 0;
+      bool ok = true;
+      for (long long t = blockIdx.x; t < total && ok; t += gridDim.x, ++i) {
+        const int b = i & 1;
+        if (i >= 2 && !(ok = mbar_wait(smem_u32(&tempty[b]), (uint32_t)(((i >> 1) - 1) & 1), a.status))) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dacc = tmem + (uint32_t)(b * BN);
+        for (int kb = 0; kb < kblocks; ++kb, ++g) {
+          const int s = (int)(g % STAGES);
+          if (!(ok = mbar_wait(smem_u32(&full[s]), (uint32_t)((g / STAGES) & 1), a.status))) break;
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = smem_u32(tiles + s * STAGE_BYTES);
+          const uint32_t sb = sa + A_BYTES;
+          const bool second = kb >= kb1;
+          const int amn = second ? a.a2_mn : a.a_mn, bmn = second ? a.b2_mn : a.b_mn;
+          const uint32_t idesc = second ? idesc2 : idesc1;
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk) {
+            // K-major: 32 bytes inside the swizzle atom; MN-major: 16 K rows of 128 bytes
+            const uint64_t ad =
+                amn ? smem_desc(sa + kk * 2048, a.lbo_mn, a.sbo_mn) : smem_desc(sa + kk * 32, 16, 1024);
+            const uint64_t bd =
+                bmn ? smem_desc(sb + kk * 2048, a.lbo_mn, a.sbo_mn) : smem_desc(sb + kk * 32, 16, 1024);
+            const uint32_t acc = (kb > 0 || kk > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(dacc),
+                "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                : "memory");
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&empty[s]))
+                       : "memory");
+        }
+        if (ok)
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&tfull[b]))
+                       : "memory");
+      }
+    }
+  } else {
+    // ------------------------------------------------ epilogue warps 0-3
+    int i = 0;
+    for (long long t = blockIdx.x; t < total; t += gridDim.x, ++i) {
+      const int bz = (int)(t / ((long long)mt * nt));
+      const int rem = (int)(t % ((long long)mt * nt));
+      const int m0 = (rem % mt) * BM, n0 = (rem / mt) * BN;
+      const int b = i & 1;
+      const bool have =
+          __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull[b]), (uint32_t)((i >> 1) & 1), a.status));
+      if (!have) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int row = m0 + warp * 32 + lane;
+      const size_t cbase = (size_t)bz * a.stride_c + (size_t)row * a.ldc;
+      const size_t rbase = (size_t)bz * a.stride_r + (size_t)row * a.ldr;
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * BN + c0);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+              "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+              "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+              "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (c0 + 32 >= BN) {
+          // the whole accumulator has been read: hand the TMEM buffer back
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
+        }
+      if (row < a.M && a.vec_ok && n0 + c0 + 32 <= a.N) {
+        // 32 consecutive columns of this thread's row: 16-byte vector loads/stores
+        const int col0 = n0 + c0;
+        float z[32];
+  #pragma unroll
+        for (int q = 0; q < 32; ++q) z[q] = __fmul_rn(a.alpha, __uint_as_float(r[q]));
+        if (a.bias) {
+  #pragma unroll
+          for (int v = 0; v < 8; ++v) {
+            const float4 b = *reinterpret_cast<const float4*>(a.bias + col0 + 4 * v);
+            z[4 * v] = __fadd_rn(z[4 * v], b.x);
+            z[4 * v + 1] = __fadd_rn(z[4 * v + 1], b.y);
+            z[4 * v + 2] = __fadd_rn(z[4 * v + 2], b.z);
+            z[4 * v + 3] = __fadd_rn(z[4 * v + 3], b.w);
+          }
+        }
+        if (a.res16) {
+  #pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const uint4 u = *reinterpret_cast<const uint4*>(a.res16 + rbase + col0 + 8 * v);
+            const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+  #pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 h2 = *reinterpret_cast<const __nv_bfloat162*>(&w[e]);
+              z[8 * v + 2 * e] = __fadd_rn(z[8 * v + 2 * e], __low2float(h2));
+              z[8 * v + 2 * e + 1] = __fadd_rn(z[8 * v + 2 * e + 1], __high2float(h2));
+            }
+          }
+        }
+        auto store_bf16 = [&](__nv_bfloat16* dst, const float* v32) {
+  #pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            uint32_t w[4];
+  #pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const __nv_bfloat162 h2 = __floats2bfloat162_rn(v32[8 * v + 2 * e], v32[8 * v + 2 * e + 1]);
+              w[e] = *reinterpret_cast<const uint32_t*>(&h2);
+            }
+            *reinterpret_cast<uint4*>(dst + 8 * v) = make_uint4(w[0], w[1], w[2], w[3]);
+          }
+        };
+        if (a.pre16) store_bf16(a.pre16 + cbase + col0, z);
+        if (a.act == 1) {
+  #pragma unroll
+          for (int q = 0; q < 32; ++q) z[q] = gelu(z[q]);
+        }
+        if (a.c32) {
+          float* dst = a.c32 + cbase + col0;
+  #pragma unroll
+          for (int v = 0; v < 8; ++v) {
+            float4 o = make_float4(z[4 * v], z[4 * v + 1], z[4 * v + 2], z[4 * v + 3]);
+            if (a.accumulate) {
+              const float4 c = *reinterpret_cast<const float4*>(dst + 4 * v);
+              o.x = __fadd_rn(o.x, c.x);
+              o.y = __fadd_rn(o.y, c.y);
+              o.z = __fadd_rn(o.z, c.z);
+              o.w = __fadd_rn(o.w, c.w);
+            }
+            *reinterpret_cast<float4*>(dst + 4 * v) = o;
+          }
+        } else {
+          __nv_bfloat16* dst = a.c16 + cbase + col0;
+          if (a.accumulate) {
+  #pragma unroll
+            for (int q = 0; q < 32; ++q) z[q] = __fadd_rn(z[q], __bfloat162float(dst[q]));
+          }
+          store_bf16(dst, z);
+        }
+      } else if (row < a.M) {
+  #pragma unroll
+        for (int q = 0; q < 32; ++q) {
+          const int col = n0 + c0 + q;
+          if (col < a.N) {
+            float z = __fmul_rn(a.alpha, __uint_as_float(r[q]));
+            if (a.bias) z = __fadd_rn(z, a.bias[col]);
+            if (a.res16) z = __fadd_rn(z, __bfloat162float(a.res16[rbase + col]));
+            if (a.pre16) a.pre16[cbase + col] = __float2bfloat16_rn(z);
+            float y = a.act == 1 ? gelu(z) : z;
+            if (a.c32) {
+              if (a.accumulate) y = __fadd_rn(y, a.c32[cbase + col]);
+              a.c32[cbase + col] = y;
+            } else {
+              if (a.accumulate) y = __fadd_rn(y, __bfloat162float(a.c16[cbase + col]));
+              a.c16[cbase + col] = __float2bfloat16_rn(y);
+            }
+          }
+        }
+      }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN) : "memory");
   }
 }
 
@@ -295,22 +428,29 @@ int make_map(CUtensorMap* tm, const void* base, uint64_t inner, uint64_t outer, 
   return r == CUDA_SUCCESS ? FDTD_OK : FDTD_ERR_ARG;
 }
 
-template <int BN>
+template <int BN, int STAGES>
 size_t smem_bytes() {
-  return 1024 + (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * STAGES + 2) + 32768;  // + guard
+  return 1024 + (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * STAGES + 5);
 }
 
-template <int BN>
-int launch_gemm_t(const CUtensorMap& ta, const CUtensorMap& tb, const GemmArgs& g, cudaStream_t st) {
-  auto kern = k_gemm<BN>;
-  const size_t smem = smem_bytes<BN>();
+template <int BN, int STAGES>
+int launch_gemm_t(const CUtensorMap& ta, const CUtensorMap& tb, const CUtensorMap& ta2, const CUtensorMap& tb2,
+                  const GemmArgs& g, cudaStream_t st) {
+  auto kern = k_gemm<BN, STAGES>;
+  const size_t smem = smem_bytes<BN, STAGES>();
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) {
     fdtd_host::note_cuda_error(e);
     return FDTD_ERR_CUDA;
   }
-  const dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.batch);
-  kern<<<grid, THREADS, smem, st>>>(ta, tb, g);
+  int dev = 0, nsm = 0, occ = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, THREADS, smem);
+  if (occ < 1) occ = 1;
+  const long long tiles = (long long)((g.M + BM - 1) / BM) * ((g.N + BN - 1) / BN) * g.batch;
+  const long long grid = std::min<long long>(tiles, (long long)nsm * occ);
+  kern<<<(unsigned)grid, THREADS, smem, st>>>(ta, tb, ta2, tb2, g);
   return fdtd_host::check_launch();
 }
 
@@ -322,7 +462,7 @@ extern "C" int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_
   if (!d || !d->A || !d->B) return FDTD_ERR_NULL;
   if (!d->C32 == !d->C16) return FDTD_ERR_ARG;  // exactly one output
   if (d->M < 1 || d->N < 1 || d->K < 1 || d->batch < 1) return FDTD_ERR_SIZE;
-  if (d->N > 65535 * 128 || d->M > 65535 * BM || d->batch > 65535) return FDTD_ERR_SIZE;
+  if (d->N > 65535 * 64 || d->batch > 65535) return FDTD_ERR_SIZE;
   auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
   if (!al16(d->A) || !al16(d->B)) return FDTD_ERR_ALIGN;
   if (d->lda % 8 || d->ldb % 8 || (d->batch > 1 && (d->stride_a % 8 || d->stride_b % 8))) return FDTD_ERR_ALIGN;
@@ -345,7 +485,32 @@ extern "C" int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_
   if (!d->b_mn_major) rc = make_map(&tb, d->B, d->K, d->N, bb, d->ldb, sb, BK, BN);
   else rc = make_map(&tb, d->B, d->N, d->K, bb, d->ldb, sb, 64, BK);
   if (rc) return rc;
+  CUtensorMap ta2 = ta, tb2 = tb;
+  int a2_sh = 0, b2_sh = 0;
+  if (d->K2 > 0) {
+    if (!d->A2 || !d->B2) return FDTD_ERR_NULL;
+    if (!al16(d->A2) || !al16(d->B2)) return FDTD_ERR_ALIGN;
+    if (d->lda2 % 8 || d->ldb2 % 8 || (d->batch > 1 && (d->stride_a2 % 8 || d->stride_b2 % 8))) return FDTD_ERR_ALIGN;
+    if ((d->a2_mn_major ? d->lda2 < d->M : d->lda2 < d->K2) || (d->b2_mn_major ? d->ldb2 < d->N : d->ldb2 < d->K2))
+      return FDTD_ERR_SIZE;
+    a2_sh = (d->batch == 1 || d->stride_a2 == 0);
+    b2_sh = (d->batch == 1 || d->stride_b2 == 0);
+    const uint64_t sa2 = a2_sh ? (uint64_t)d->lda2 * (d->a2_mn_major ? d->K2 : d->M) : (uint64_t)d->stride_a2;
+    const uint64_t sb2 = b2_sh ? (uint64_t)d->ldb2 * (d->b2_mn_major ? d->K2 : d->N) : (uint64_t)d->stride_b2;
+    const uint64_t ba2 = a2_sh ? 1 : (uint64_t)d->batch, bb2 = b2_sh ? 1 : (uint64_t)d->batch;
+    if (!d->a2_mn_major) rc = make_map(&ta2, d->A2, d->K2, d->M, ba2, d->lda2, sa2, BK, BM);
+    else rc = make_map(&ta2, d->A2, d->M, d->K2, ba2, d->lda2, sa2, 64, BK);
+    if (rc) return rc;
+    if (!d->b2_mn_major) rc = make_map(&tb2, d->B2, d->K2, d->N, bb2, d->ldb2, sb2, BK, BN);
+    else rc = make_map(&tb2, d->B2, d->N, d->K2, bb2, d->ldb2, sb2, 64, BK);
+    if (rc) return rc;
+  }
   GemmArgs g{};
+  g.K2 = d->K2 > 0 ? d->K2 : 0;
+  g.a2_mn = d->a2_mn_major;
+  g.b2_mn = d->b2_mn_major;
+  g.a2_shared = a2_sh;
+  g.b2_shared = b2_sh;
   g.M = d->M;
   g.N = d->N;
   g.K = d->K;
@@ -366,9 +531,20 @@ extern "C" int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_
   g.pre16 = reinterpret_cast<__nv_bfloat16*>(d->pre16);
   g.lbo_mn = d->mn_lbo ? (unsigned)d->mn_lbo : (unsigned)(BK * 128);
   g.sbo_mn = d->mn_sbo ? (unsigned)d->mn_sbo : 1024u;
+  {
+    const void* cptr = d->C32 ? (const void*)d->C32 : d->C16;
+    bool v = al16(cptr) && d->ldc % 8 == 0 && d->stride_c % 8 == 0;
+    if (d->bias) v = v && al16(d->bias);
+    if (d->res16) v = v && al16(d->res16) && d->ldr % 8 == 0 && d->stride_r % 8 == 0;
+    if (d->pre16) v = v && al16(d->pre16);
+    g.vec_ok = v ? 1 : 0;
+  }
   g.a_shared = a_sh ? 1 : 0;
   g.b_shared = b_sh ? 1 : 0;
   g.status = status;
-  if (BN == 64) return launch_gemm_t<64>(ta, tb, g, (cudaStream_t)stream);
-  return launch_gemm_t<128>(ta, tb, g, (cudaStream_t)stream);
+  const bool deep = d->K + g.K2 > 2 * BK;  // pipeline depth: 4 stages for long K, 2 for short K
+  cudaStream_t st = (cudaStream_t)stream;
+  if (BN == 64)
+    return deep ? launch_gemm_t<64, 4>(ta, tb, ta2, tb2, g, st) : launch_gemm_t<64, 2>(ta, tb, ta2, tb2, g, st);
+  return deep ? launch_gemm_t<128, 4>(ta, tb, ta2, tb2, g, st) : launch_gemm_t<128, 2>(ta, tb, ta2, tb2, g, st);
 }

@@ -24,7 +24,9 @@ def _ld_stride(t: torch.Tensor):
 def gemm(A: torch.Tensor, B: torch.Tensor, *, a_mn: bool = False, b_mn: bool = False, out: torch.Tensor | None = None,
          out_dtype=torch.float32, bias: torch.Tensor | None = None, residual: torch.Tensor | None = None,
          alpha: float = 1.0, gelu: bool = False, accumulate: bool = False, pre: torch.Tensor | None = None,
-         status: torch.Tensor | None = None, mn_lbo: int = 0, mn_sbo: int = 0) -> torch.Tensor:
+         status: torch.Tensor | None = None, mn_lbo: int = 0, mn_sbo: int = 0, second=None) -> torch.Tensor:
+    """``second`` = (A2, B2, a2_mn, b2_mn) adds A2 @ B2' to the accumulator before
+    the epilogue (same output shape)."""
     for t in (A, B):
         if t.dtype != torch.bfloat16 or not t.is_cuda:
             raise TypeError("A and B must be BF16 CUDA tensors")
@@ -63,6 +65,17 @@ def gemm(A: torch.Tensor, B: torch.Tensor, *, a_mn: bool = False, b_mn: bool = F
         d.pre16 = pre.data_ptr()
     d.alpha, d.act, d.accumulate = float(alpha), int(gelu), int(accumulate)
     d.mn_lbo, d.mn_sbo = mn_lbo, mn_sbo
+    if second is not None:
+        A2, B2, a2_mn, b2_mn = second
+        K2 = A2.shape[-2] if a2_mn else A2.shape[-1]
+        K2b = B2.shape[-2] if b2_mn else B2.shape[-1]
+        if K2 != K2b:
+            raise ValueError(f"second product: inner dimensions differ: {K2} vs {K2b}")
+        la2, sa2, _ = _ld_stride(A2)
+        lb2, sb2, _ = _ld_stride(B2)
+        d.K2 = K2
+        d.A2, d.lda2, d.stride_a2, d.a2_mn_major = A2.data_ptr(), la2, sa2, int(a2_mn)
+        d.B2, d.ldb2, d.stride_b2, d.b2_mn_major = B2.data_ptr(), lb2, sb2, int(b2_mn)
     st = None if status is None else status.data_ptr()
     _lib.call("fdtd_gemm_bf16", C.byref(d), st, _lib.stream_ptr())
     return out

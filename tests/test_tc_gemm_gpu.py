@@ -42,7 +42,7 @@ def test_gemm_batched_shared_and_epilogue(cuda_lib):
     torch.cuda.synchronize()
     z = 0.5 * (A.float().transpose(1, 2) @ Bs.float().T) + bias + res.float()
     assert _rel(pre, z) <= 1e-2
-    assert _rel(out, torch.nn.functional.gelu(z)) <= 1e-2
+    assert _rel(out, torch.nn.functional.gelu(z, approximate="tanh")) <= 1e-2
     acc = torch.randn(nb, M, N, device="cuda", generator=g)
     ref = acc + A.float().transpose(1, 2) @ Bs.float().T
     tc.gemm(A, Bs.unsqueeze(0).expand(nb, -1, -1), a_mn=True, out=acc, accumulate=True)
@@ -59,3 +59,20 @@ def test_gemm_rejects_unaligned_leading_dimension(cuda_lib):
     with pytest.raises(_lib.FdtdError) as e:
         tc.gemm(A, B, a_mn=True)
     assert e.value.code == -3
+
+
+def test_gemm_second_product_shares_the_accumulator(cuda_lib):
+    """acc = A.B^T + A2.B2' with a batched A, a shared B, a shared MN-major A2
+    and a batched B2, then bias + GELU: the fused inverse-DFT + pointwise layer."""
+    from simulation_gb300 import tc
+    g = torch.Generator(device="cuda").manual_seed(11)
+    nb, M, N, K, K2 = 3, 256, 128, 128, 64
+    A = torch.randn(nb, M, K, device="cuda", generator=g).bfloat16()
+    W = torch.randn(N, K, device="cuda", generator=g).bfloat16()
+    A2t = torch.randn(K2, M, device="cuda", generator=g).bfloat16()     # stored transposed
+    B2 = torch.randn(nb, N, K2, device="cuda", generator=g).bfloat16()
+    bias = torch.randn(N, device="cuda", generator=g)
+    out = tc.gemm(A, W, bias=bias, gelu=True, out_dtype=torch.bfloat16, second=(A2t, B2, True, False))
+    torch.cuda.synchronize()
+    z = A.float() @ W.float().T + A2t.float().T @ B2.float().transpose(1, 2) + bias
+    assert _rel(out, torch.nn.functional.gelu(z, approximate="tanh")) <= 1e-2
