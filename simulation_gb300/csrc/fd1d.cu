@@ -131,8 +131,8 @@ constexpr int RUN1D_MAX_THREADS = 1024;
 // block size limit per cells-per-thread, so the register budget grows with CPT
 __host__ __device__ constexpr int run1d_max_threads(int cpt) { return cpt <= 8 ? 1024 : 512; }
 
-template <int FORM, int CPT, bool CLUSTER>
-__global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1DArgs a) {
+template <int FORM, int CPT, bool CLUSTER, bool ONE_WARP>
+__global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d_run(const Run1DArgs a) {
   const fdtd1d_params& p = a.p;
   const fdtd1d_state& s = a.s;
   __shared__ float x_first_ex[RUN1D_MAX_THREADS];
@@ -150,8 +150,10 @@ __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1D
   }
   auto sync_all = [&]() {
     if (CLUSTER) cg::this_cluster().sync();
+    else if (ONE_WARP) __syncwarp();
     else __syncthreads();
   };
+  const int lane = tid & 31, w = tid >> 5, nw = T >> 5;
   auto remote = [&](float* base, int r, int idx) -> float {
     if (CLUSTER) {
       float* rp = cg::this_cluster().map_shared_rank(base, r);
@@ -176,6 +178,35 @@ __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1D
     ixa[c] = (DF && in) ? s.ix[g] : 0.f;
     sxa[c] = (FORM == FDTD1D_FORM_DEBYE && in) ? s.sx[g] : 0.f;
   }
+  // per-cell coefficients: in registers for the whole run when the register
+  // budget allows (one warp, or few cells per thread), else read from L1 each step
+  constexpr bool KREG = ONE_WARP || CPT <= 4;
+  float k0[CPT], k1[CPT], k2[CPT], k3[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) {
+    const int g = g0 + c;
+    const bool in = g >= 1 && g < nx;
+    k0[c] = k1[c] = k2[c] = k3[c] = 0.f;
+    if (KREG && in) {
+      if (FORM == FDTD1D_FORM_CB) k0[c] = __ldg(p.cb + g);
+      if (FORM == FDTD1D_FORM_CACB) {
+        k0[c] = __ldg(p.ca + g);
+        k1[c] = __ldg(p.cb + g);
+      }
+      if (DF) {
+        k0[c] = __ldg(p.nax + g);
+        k1[c] = __ldg(p.nbx + g);
+      }
+      if (FORM == FDTD1D_FORM_DEBYE) {
+        k2[c] = __ldg(p.ncx + g);
+        k3[c] = __ldg(p.ndx + g);
+      }
+    }
+  }
+  // the source value of the next step is fetched one step ahead
+  const bool have_src = p.src_kind != FDTD_SRC_NONE;
+  const bool src_here = have_src && p.src_k >= g0 && p.src_k < g0 + CPT;
+  float v_next = (src_here && a.nsteps > 0) ? __ldg(p.src_table + a.t0) : 0.f;
   // ABC owners: gthr 0 (cells 0,1 since CPT >= 2) and the thread of cell nx-1
   const bool own_lo = p.abc && gthr == 0;
   const int hi_thr = (nx - 1) / CPT;
@@ -208,38 +239,46 @@ __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1D
       }
   }
 
-  x_last_hy[tid] = hy[CPT - 1];
+  // neighbour values travel by warp shuffle; only a warp's edge lanes go
+  // through shared memory (one slot per warp) or, across blocks, through
+  // distributed shared memory
+  if (lane == 31) x_last_hy[w] = hy[CPT - 1];
   sync_all();
 
   for (int t = a.t0 + 1; t <= a.t0 + a.nsteps; ++t) {
     // ---------------- E stage
-    float hy_left = 0.f;
-    if (tid > 0) hy_left = x_last_hy[tid - 1];
-    else if (rank > 0) hy_left = remote(x_last_hy, rank - 1, T - 1);
-    const float v = (p.src_kind != FDTD_SRC_NONE) ? __ldg(p.src_table + t - 1) : 0.f;
+    float hy_left = __shfl_up_sync(0xffffffffu, hy[CPT - 1], 1);
+    if (lane == 0) {
+      if (w > 0) hy_left = x_last_hy[w - 1];
+      else if (rank > 0) hy_left = remote(x_last_hy, rank - 1, nw - 1);
+      else hy_left = 0.f;
+    }
+    const float v = v_next;
+    if (src_here && t < a.t0 + a.nsteps) v_next = __ldg(p.src_table + t);
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const int g = g0 + c;
       const float hym = (c == 0) ? hy_left : hy[c - 1];
       if (g >= 1 && g < nx) {
         if (FORM == FDTD1D_FORM_CB) {
-          ex[c] = ex_update_cb(ex[c], hym, hy[c], __ldg(p.cb + g));
+          ex[c] = ex_update_cb(ex[c], hym, hy[c], KREG ? k0[c] : __ldg(p.cb + g));
         } else if (FORM == FDTD1D_FORM_CACB) {
-          ex[c] = ex_update_cacb(ex[c], hym, hy[c], __ldg(p.ca + g), __ldg(p.cb + g));
+          ex[c] = ex_update_cacb(ex[c], hym, hy[c], KREG ? k0[c] : __ldg(p.ca + g), KREG ? k1[c] : __ldg(p.cb + g));
         } else {
           dx[c] = dx_update(dx[c], hym, hy[c]);
         }
       }
-      if (p.src_kind != FDTD_SRC_NONE && g == p.src_k) {
+      if (src_here && g == p.src_k) {
         if (DF) dx[c] = (p.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(dx[c], v);
         else ex[c] = (p.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(ex[c], v);
       }
       if (DF && g >= 1 && g < nx) {
         if (FORM == FDTD1D_FORM_DFORM)
-          ex[c] = ex_from_dx(dx[c], ixa[c], __ldg(p.nax + g), __ldg(p.nbx + g));
+          ex[c] = ex_from_dx(dx[c], ixa[c], KREG ? k0[c] : __ldg(p.nax + g), KREG ? k1[c] : __ldg(p.nbx + g));
         else
-          ex[c] = ex_from_dx_debye(dx[c], ixa[c], sxa[c], __ldg(p.nax + g), __ldg(p.nbx + g), __ldg(p.ncx + g),
-                                   __ldg(p.ndx + g));
+          ex[c] = ex_from_dx_debye(dx[c], ixa[c], sxa[c], KREG ? k0[c] : __ldg(p.nax + g),
+                                   KREG ? k1[c] : __ldg(p.nbx + g), KREG ? k2[c] : __ldg(p.ncx + g),
+                                   KREG ? k3[c] : __ldg(p.ndx + g));
       }
     }
     // running DFT: probes published here, full field accumulated in place
@@ -282,8 +321,10 @@ __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1D
       for (int c = 0; c < CPT; ++c)
         if (c == hi_c) ex[c] = bc3;
     }
-    x_first_ex[tid] = ex[0];
-    x_last_ex[tid] = ex[CPT - 1];
+    const float prev_last_ex = __shfl_up_sync(0xffffffffu, ex[CPT - 1], 1);
+    const float next_first_ex = __shfl_down_sync(0xffffffffu, ex[0], 1);
+    if (lane == 0) x_first_ex[w] = ex[0];
+    if (lane == 31) x_last_ex[w] = ex[CPT - 1];
     sync_all();  // barrier A
 
     // ---------------- H stage
@@ -294,10 +335,12 @@ __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1D
 #pragma unroll
         for (int c = 1; c < CPT; ++c)
           if (c == hi_c) e_nm2 = ex[c - 1];
-      } else if (tid > 0) {
-        e_nm2 = x_last_ex[tid - 1];
+      } else if (lane > 0) {
+        e_nm2 = prev_last_ex;
+      } else if (w > 0) {
+        e_nm2 = x_last_ex[w - 1];
       } else {
-        e_nm2 = remote(x_last_ex, rank - 1, T - 1);
+        e_nm2 = remote(x_last_ex, rank - 1, nw - 1);
       }
       bc3 = bc2;
       bc2 = e_nm2;
@@ -313,15 +356,18 @@ __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1D
           pr_i[q] = __fmaf_rn(-sf, e, pr_i[q]);
         }
     }
-    float ex_right = 0.f;
-    if (tid < T - 1) ex_right = x_first_ex[tid + 1];
-    else if (rank < C - 1) ex_right = remote(x_first_ex, rank + 1, 0);
+    float ex_right = next_first_ex;
+    if (lane == 31) {
+      if (w + 1 < nw) ex_right = x_first_ex[w + 1];
+      else if (rank < C - 1) ex_right = remote(x_first_ex, rank + 1, 0);
+      else ex_right = 0.f;
+    }
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const int g = g0 + c;
       if (g <= nx - 2) hy[c] = hy_update(hy[c], ex[c], (c == CPT - 1) ? ex_right : ex[c + 1]);
     }
-    x_last_hy[tid] = hy[CPT - 1];
+    if (lane == 31) x_last_hy[w] = hy[CPT - 1];
     sync_all();  // barrier B
   }
 
@@ -361,9 +407,9 @@ __global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1D
 // ============================================================ launchers
 namespace {
 
-template <int FORM, int CPT, bool CLUSTER>
+template <int FORM, int CPT, bool CLUSTER, bool ONE_WARP>
 int launch_run_t(const Run1DArgs& a, int threads, int cluster, cudaStream_t st) {
-  auto kern = k_fd1d_run<FORM, CPT, CLUSTER>;
+  auto kern = k_fd1d_run<FORM, CPT, CLUSTER, ONE_WARP>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster, 1, 1);
   cfg.blockDim = dim3(threads, 1, 1);
@@ -391,14 +437,15 @@ int launch_run_t(const Run1DArgs& a, int threads, int cluster, cudaStream_t st) 
 template <int FORM, int CPT>
 int regs_of() {
   cudaFuncAttributes fa{};
-  if (cudaFuncGetAttributes(&fa, k_fd1d_run<FORM, CPT, true>) != cudaSuccess) return 255;
+  if (cudaFuncGetAttributes(&fa, k_fd1d_run<FORM, CPT, true, false>) != cudaSuccess) return 255;
   return fa.numRegs;
 }
 
 template <int FORM, int CPT>
 int launch_run_cpt(const Run1DArgs& a, int threads, int cluster, cudaStream_t st) {
-  if (cluster > 1) return launch_run_t<FORM, CPT, true>(a, threads, cluster, st);
-  return launch_run_t<FORM, CPT, false>(a, threads, cluster, st);
+  if (cluster > 1) return launch_run_t<FORM, CPT, true, false>(a, threads, cluster, st);
+  if (threads == 32) return launch_run_t<FORM, CPT, false, true>(a, threads, cluster, st);
+  return launch_run_t<FORM, CPT, false, false>(a, threads, cluster, st);
 }
 
 template <int FORM>
@@ -417,6 +464,16 @@ int launch_run_form(const Run1DArgs& a, cudaStream_t st) {
     t = (t / 32) * 32;
     return std::min(t, run1d_max_threads(cpt));
   };
+  // a line of up to 512 cells runs in ONE warp (no block barrier at all)
+  if (nx <= 32 * 16) {
+    const int cpt = nx <= 64 ? 2 : nx <= 128 ? 4 : nx <= 256 ? 8 : 16;
+    switch (cpt) {
+      case 2: return launch_run_cpt<FORM, 2>(a, 32, 1, st);
+      case 4: return launch_run_cpt<FORM, 4>(a, 32, 1, st);
+      case 8: return launch_run_cpt<FORM, 8>(a, 32, 1, st);
+      default: return launch_run_cpt<FORM, 16>(a, 32, 1, st);
+    }
+  }
   for (int pass = 0; pass < 3; ++pass) {
     const int limit_threads = pass == 0 ? 256 : RUN1D_MAX_THREADS;
     for (const Cand& c : cands) {
