@@ -63,6 +63,15 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _peaks_bf16():
+    """Dense BF16 TFLOP/s measured as a burst (the surrogate pass is timed alone)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["bf16_tflops"])
+    except Exception:
+        return 1900.0
+
+
 class Clocks:
     """nvidia-smi sampling during the timed region."""
 
@@ -328,7 +337,56 @@ def run_secondary(args, st, world) -> dict:
                                            "spectra_per_s": batch.nruns / ms * 1e3, "tuning": tuned["tuning"],
                                            "status": int(runner.status.item()),
                                            "runs_done": int(runner.done.sum().item())}
+    del runner
+    out["adjoint_1024sq_3000steps"] = _bench_adjoint(st)
+    out["surrogate_fno_batch65536"] = _bench_surrogate(st, batch.nruns / ms * 1e3)
+    torch.cuda.empty_cache()
     return out
+
+
+def _bench_adjoint(st) -> dict:
+    """Gradient of J = sum_t Ez(probe)^2 w.r.t. eps_r on a 256^2 design box of a
+    1024^2 lossy PML grid, 3000 steps, checkpoint every 64 steps."""
+    import torch
+
+    from simulation_gb300 import adjoint as A
+    pr, eps = A.design_problem(seed=0)
+    pr.set_eps(eps)
+    pr.forward()
+    pr.gradient_eps()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    ev[0].record(st)
+    pr.forward()
+    ev[1].record(st)
+    pr.gradient_eps()
+    ev[2].record(st)
+    torch.cuda.synchronize()
+    fwd, rev = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    cu = pr.nx * pr.ny * pr.ns
+    res = {"forward_ms": fwd, "reverse_ms": rev, "forward_Gcell_updates_per_s": cu / fwd / 1e6,
+           "reverse_Gcell_updates_per_s": cu / rev / 1e6, "checkpoint": pr.cp}
+    del pr
+    return res
+
+
+def _bench_surrogate(st, fdtd_spectra_per_s: float) -> dict:
+    """Served surrogate (network, propagation frame, product) at batch 65536;
+    throughput does not depend on the weights, so a seeded untrained network
+    is timed.  Tensor-core FLOPs against the measured dense BF16 peak."""
+    import torch
+
+    from simulation_gb300 import surrogate as S
+    m = S.FNO(seed=0)
+    sps = S.time_inference(m, n=65536, chunk=4096, reps=1)
+    fl = S.flops_per_sample(m)
+    peak = _peaks_bf16()
+    res = {"spectra_per_s": sps, "gflop_per_sample": fl / 1e9, "tflops": sps * fl / 1e12,
+           "frac_of_bf16_peak": None if peak is None else sps * fl / 1e12 / peak,
+           "vs_batched_fdtd_spectra_per_s": sps / fdtd_spectra_per_s}
+    del m
+    torch.cuda.empty_cache()
+    return res
 
 
 def run_e2e(sim, args, st, world, dev) -> dict:

@@ -257,10 +257,22 @@ int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_t stream);
  * (no reference counterpart); BF16 tensors are passed as void*.  Shapes:
  * rows = B*N positions, C channels, M retained modes, DFT layout [B][C][2M]
  * (cos rows, then -sin rows), mode-major layout [M][B][2C] ([Re | Im]). */
-int fno_lift_fwd(long long rows, int C, const float* in, const float* P, const float* p, void* x0,
+/* lift from cin <= 8 input channels per position: x0 = in P^T + p */
+int fno_lift_fwd(long long rows, int C, int cin, const float* in, const float* P, const float* p, void* x0,
                  fdtd_stream_t stream);
-int fno_lift_bwd(long long rows, int C, const float* in, const void* dx0, float* dP, float* dp,
+int fno_lift_bwd(long long rows, int C, int cin, const float* in, const void* dx0, float* dP, float* dp,
                  fdtd_stream_t stream);
+/* Propagation frame of a slab profile: feat [n][nbins][6] = (eps_r-1)/eps_scale of
+ * cells 2b-1, 2b, 2b+1 then sigma/sig_scale of the same cells (vacuum = 0);
+ * P [n][2*nf] = [Re | Im] of exp(-i sum k(f, cell)) over the cells from probe_in
+ * to probe_gap cells behind the last non-vacuum cell, k the complex wavenumber of
+ * the lossy 1D Yee update (fd1d/program/fd1d_1_5.py:37-44, :65, :72) at w*dt =
+ * wdt[f] (double, device); loss_scale = dt/(2 eps0). */
+int fno_propagation(int n, int nbins, const float* feat, int nf, const double* wdt, double eps_scale,
+                    double sig_scale, double loss_scale, int probe_in, int probe_gap, float* P,
+                    fdtd_stream_t stream);
+/* out = P (.) y, or conj(P) (.) y when conj_p, for n spectra stored [Re(nf) | Im(nf)] */
+int fno_cmul(long long n, int nf, const float* P, const float* y, int conj_p, float* out, fdtd_stream_t stream);
 int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_t stream);
 int fno_modes_to_dft(int B, int C, int M, const float* Gm, void* G, fdtd_stream_t stream);
 int fno_build_rbig(int M, int C, const float* Rr, const float* Ri, void* Rbig, fdtd_stream_t stream);

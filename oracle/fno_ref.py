@@ -27,7 +27,7 @@ def gelu(z):
 
 
 def forward(params: dict, inp: torch.Tensor, layers: int, modes: int) -> torch.Tensor:
-    """params: name -> float64 tensor; inp [B][N][2] float64 -> out [B][D]."""
+    """params: name -> float64 tensor; inp [B][N][cin] float64 -> out [B][D]."""
     B, N, _ = inp.shape
     phi, psi = dft_matrices(N, modes)
     x = inp @ params["P"].T + params["pb"]                       # [B][N][C]
@@ -45,9 +45,26 @@ def forward(params: dict, inp: torch.Tensor, layers: int, modes: int) -> torch.T
     return a1 @ params["H2"].T + params["hb2"]
 
 
-def loss_and_grads(params: dict, inp: torch.Tensor, target: torch.Tensor, layers: int, modes: int):
+def apply_frame(frame: torch.Tensor, y: torch.Tensor) -> torch.Tensor:
+    """T = P (.) y for spectra stored [Re | Im]."""
+    nf = y.shape[1] // 2
+    pr, pi, yr, yi = frame[:, :nf], frame[:, nf:], y[:, :nf], y[:, nf:]
+    return torch.cat([pr * yr - pi * yi, pr * yi + pi * yr], dim=1)
+
+
+def loss_and_grads(params: dict, inp: torch.Tensor, target: torch.Tensor, layers: int, modes: int,
+                   frame: torch.Tensor | None = None, rel_floor2: float | None = None):
+    """Loss, network output and parameter gradients.  ``frame``: loss on
+    P (.) y; ``rel_floor2``: per-sample ||o-t||^2 / max(||t||^2, floor2)
+    averaged over the batch, else the plain mean squared error."""
     p = {k: v.detach().double().cpu().clone().requires_grad_(True) for k, v in params.items()}
     o = forward(p, inp.double().cpu(), layers, modes)
-    loss = ((o - target.double().cpu()) ** 2).mean()
+    out = o if frame is None else apply_frame(frame.double().cpu(), o)
+    t = target.double().cpu()
+    if rel_floor2 is None:
+        loss = ((out - t) ** 2).mean()
+    else:
+        w = 1.0 / torch.clamp((t ** 2).sum(1), min=rel_floor2)
+        loss = (w * ((out - t) ** 2).sum(1)).mean()
     grads = torch.autograd.grad(loss, list(p.values()))
     return float(loss), o.detach(), {k: g for k, g in zip(p.keys(), grads)}

@@ -137,8 +137,11 @@ _SIGS = {
     "fdtd1d_fourier": ([C.c_int, C.POINTER(Params1D), C.POINTER(State1D), P], C.c_int),
     "fdtd1d_step_n": ([C.POINTER(Params1D), C.POINTER(State1D), C.c_int, C.c_int, P], C.c_int),
     "fdtd_gemm_bf16": ([C.POINTER(GemmDesc), P, P], C.c_int),
-    "fno_lift_fwd": ([C.c_longlong, C.c_int, F, F, F, P, P], C.c_int),
-    "fno_lift_bwd": ([C.c_longlong, C.c_int, F, P, F, F, P], C.c_int),
+    "fno_lift_fwd": ([C.c_longlong, C.c_int, C.c_int, F, F, F, P, P], C.c_int),
+    "fno_lift_bwd": ([C.c_longlong, C.c_int, C.c_int, F, P, F, F, P], C.c_int),
+    "fno_propagation": ([C.c_int, C.c_int, F, C.c_int, P, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, F, P],
+                        C.c_int),
+    "fno_cmul": ([C.c_longlong, C.c_int, F, F, C.c_int, F, P], C.c_int),
     "fno_dft_to_modes": ([C.c_int, C.c_int, C.c_int, F, P, P], C.c_int),
     "fno_modes_to_dft": ([C.c_int, C.c_int, C.c_int, F, P, P], C.c_int),
     "fno_build_rbig": ([C.c_int, C.c_int, F, F, P, P], C.c_int),

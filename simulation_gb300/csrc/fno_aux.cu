@@ -36,38 +36,169 @@ inline dim3 grid1(size_t n, int t = 256) {
   return dim3((unsigned)b);
 }
 
-// lift: x0[r][c] = P[c][0]*in[r][0] + P[c][1]*in[r][1] + p[c]   (r = b*N + n)
-__global__ void k_lift_fwd(size_t rows, int C, const float* __restrict__ in, const float* __restrict__ P,
+// lift: x0[r][c] = sum_j P[c][j]*in[r][j] + p[c]   (r = b*N + n, j < cin)
+__global__ void k_lift_fwd(size_t rows, int C, int cin, const float* __restrict__ in, const float* __restrict__ P,
                            const float* __restrict__ p, bf16* __restrict__ x0) {
   const size_t total = rows * C;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     const size_t r = i / C;
     const int c = (int)(i % C);
-    const float v = fmaf(P[2 * c], in[2 * r], fmaf(P[2 * c + 1], in[2 * r + 1], p[c]));
+    float v = p[c];
+    for (int j = 0; j < cin; ++j) v = fmaf(P[c * cin + j], in[r * cin + j], v);
     x0[i] = __float2bfloat16_rn(v);
   }
 }
 
+constexpr int kLiftMaxIn = 8;
+
 // dP[c][j] += sum_r dx0[r][c]*in[r][j]; dp[c] += sum_r dx0[r][c]   (block per channel group)
-__global__ void k_lift_bwd(size_t rows, int C, const float* __restrict__ in, const bf16* __restrict__ dx0,
+__global__ void k_lift_bwd(size_t rows, int C, int cin, const float* __restrict__ in, const bf16* __restrict__ dx0,
                            float* __restrict__ dP, float* __restrict__ dp) {
   const int c = blockIdx.y;
-  float s0 = 0.f, s1 = 0.f, sb = 0.f;
+  float s[kLiftMaxIn], sb = 0.f;
+#pragma unroll
+  for (int j = 0; j < kLiftMaxIn; ++j) s[j] = 0.f;
   for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < rows; r += (size_t)gridDim.x * blockDim.x) {
     const float d = __bfloat162float(dx0[r * C + c]);
-    s0 = fmaf(d, in[2 * r], s0);
-    s1 = fmaf(d, in[2 * r + 1], s1);
+#pragma unroll
+    for (int j = 0; j < kLiftMaxIn; ++j)
+      if (j < cin) s[j] = fmaf(d, in[r * cin + j], s[j]);
     sb += d;
   }
   for (int o = 16; o > 0; o >>= 1) {
-    s0 += __shfl_down_sync(0xffffffffu, s0, o);
-    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+#pragma unroll
+    for (int j = 0; j < kLiftMaxIn; ++j) s[j] += __shfl_down_sync(0xffffffffu, s[j], o);
     sb += __shfl_down_sync(0xffffffffu, sb, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&dP[2 * c], s0);
-    atomicAdd(&dP[2 * c + 1], s1);
+#pragma unroll
+    for (int j = 0; j < kLiftMaxIn; ++j)
+      if (j < cin) atomicAdd(&dP[c * cin + j], s[j]);
     atomicAdd(&dp[c], sb);
+  }
+}
+
+// ------------------------------------------------------------ propagation frame
+// The surrogate predicts the spectrum in the frame of the single-pass
+// propagation factor P(f) = exp(-i sum_cells k(f, cell)) from the entry probe
+// to the exit probe, where k is the complex wavenumber of the 1D Yee update
+// ex = ca ex + cb (hy[k-1] - hy[k]), hy += 0.5 (ex[k] - ex[k+1]) for a plane
+// wave exp(i(w t - k x)):   sin^2(k/2) = (z^1/2 - ca z^-1/2) sin(w dt/2) / (i cb),
+// z = exp(i w dt).  The branch is the wave travelling to the right, Re k > 0
+// (in a passive cell that root also decays, Im k <= 0; choosing by the sign
+// of Im k instead would let rounding flip lossless cells).  Double precision:
+// the phase reaches thousands of radians and must stay within a small
+// fraction of one.
+struct cdbl {
+  double re, im;
+};
+__device__ __forceinline__ cdbl c_mul(cdbl a, cdbl b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+__device__ __forceinline__ cdbl c_sqrt(cdbl a) {
+  const double r = hypot(a.re, a.im);
+  const double re = sqrt(0.5 * (r + a.re));
+  const double im = copysign(sqrt(0.5 * fmax(r - a.re, 0.0)), a.im);
+  return {re, im};
+}
+// asin(q) = -i log(i q + sqrt(1 - q^2))
+__device__ __forceinline__ cdbl c_asin(cdbl q) {
+  const cdbl q2 = c_mul(q, q);
+  const cdbl r = c_sqrt({1.0 - q2.re, -q2.im});
+  const cdbl w = {r.re - q.im, r.im + q.re};
+  return {atan2(w.im, w.re), -log(hypot(w.re, w.im))};
+}
+__device__ cdbl yee_wavenumber(double ca, double cb, double wdt) {
+  const double s = sin(0.5 * wdt), c = cos(0.5 * wdt);
+  // (z^1/2 - ca z^-1/2) = c (1 - ca) + i s (1 + ca);  divided by i cb, times s
+  const cdbl Q = {s * s * (1.0 + ca) / cb, -s * c * (1.0 - ca) / cb};
+  const cdbl h = c_asin(c_sqrt(Q));
+  cdbl k = {2.0 * h.re, 2.0 * h.im};
+  if (k.re < 0.0 || (k.re == 0.0 && k.im > 0.0)) k = {-k.re, -k.im};
+  return k;
+}
+
+// Profile features, 6 channels per bin b: (eps_r - 1)/eps_scale of cells
+// 2b-1, 2b, 2b+1, then sigma/sig_scale of the same cells; vacuum is all zero.
+__device__ __forceinline__ void cell_material(const float* __restrict__ f, int nbins, int c, float& e, float& s) {
+  if (c < 0 || c >= 2 * nbins) {
+    e = 0.f;
+    s = 0.f;
+    return;
+  }
+  const float* b = f + (size_t)(c >> 1) * 6;
+  e = b[1 + (c & 1)];
+  s = b[4 + (c & 1)];
+}
+
+// one warp per sample; lane l handles frequencies l and l + 32
+__global__ void k_propagation(int n, int nbins, const float* __restrict__ feat, int nf, const double* __restrict__ wdt,
+                              double eps_scale, double sig_scale, double loss_scale, int probe_in, int probe_gap,
+                              float* __restrict__ P) {
+  const int sample = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (sample >= n) return;
+  const float* f = feat + (size_t)sample * nbins * 6;
+  int last = -1;
+  for (int c = lane; c < 2 * nbins; c += 32) {
+    float e, s;
+    cell_material(f, nbins, c, e, s);
+    if (e != 0.f || s != 0.f) last = c;
+  }
+  for (int o = 16; o > 0; o >>= 1) last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+  const int probe_out = max(last + 1, probe_in) + probe_gap;
+  double w[2];
+  bool on[2];
+  for (int q = 0; q < 2; ++q) {
+    on[q] = lane + 32 * q < nf;
+    w[q] = on[q] ? wdt[lane + 32 * q] : 0.0;
+  }
+  cdbl K[2] = {{0.0, 0.0}, {0.0, 0.0}}, kc[2] = {{0.0, 0.0}, {0.0, 0.0}};
+  float ce = -1.f, cs = -1.f;
+  int run = 0;
+  for (int c = probe_in; c < probe_out; ++c) {
+    float e, s;
+    cell_material(f, nbins, c, e, s);
+    if (e != ce || s != cs) {  // warp-uniform: every lane reads the same cell
+      for (int q = 0; q < 2; ++q) {
+        K[q].re += run * kc[q].re;
+        K[q].im += run * kc[q].im;
+      }
+      run = 0;
+      ce = e;
+      cs = s;
+      // the FDTD's float32 coefficients (lossy layer formula of fd1d/program/fd1d_1_5.py:37-44)
+      const double er = 1.0 + eps_scale * (double)e, sg = sig_scale * (double)s;
+      const double eaf = loss_scale * sg / er;
+      const double ca = (double)(float)((1.0 - eaf) / (1.0 + eaf));
+      const double cb = (double)(float)(0.5 / (er * (1.0 + eaf)));
+      for (int q = 0; q < 2; ++q) kc[q] = on[q] ? yee_wavenumber(ca, cb, w[q]) : cdbl{0.0, 0.0};
+    }
+    ++run;
+  }
+  for (int q = 0; q < 2; ++q) {
+    K[q].re += run * kc[q].re;
+    K[q].im += run * kc[q].im;
+    if (!on[q]) continue;
+    // P = exp(-i K) = exp(Im K) (cos Re K - i sin Re K)
+    const double a = exp(K[q].im);
+    double sn, cn;
+    sincos(K[q].re, &sn, &cn);
+    P[(size_t)sample * 2 * nf + lane + 32 * q] = (float)(a * cn);
+    P[(size_t)sample * 2 * nf + nf + lane + 32 * q] = (float)(-a * sn);
+  }
+}
+
+// out = P (.) y  or conj(P) (.) y per sample, spectra stored [Re(nf) | Im(nf)]
+__global__ void k_cmul(size_t n, int nf, const float* __restrict__ P, const float* __restrict__ y, int conj_p,
+                       float* __restrict__ out) {
+  const size_t total = n * nf;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t b = i / nf;
+    const int k = (int)(i % nf);
+    const size_t o = b * 2 * nf + k;
+    const float pr = P[o], pi = conj_p ? -P[o + nf] : P[o + nf];
+    const float yr = y[o], yi = y[o + nf];
+    out[o] = fmaf(pr, yr, -pi * yi);
+    out[o + nf] = fmaf(pr, yi, pi * yr);
   }
 }
 
@@ -276,18 +407,35 @@ using fdtd::bf16;
 
 extern "C" {
 
-int fno_lift_fwd(long long rows, int C, const float* in, const float* P, const float* p, void* x0,
+int fno_lift_fwd(long long rows, int C, int cin, const float* in, const float* P, const float* p, void* x0,
                  fdtd_stream_t stream) {
   if (!in || !P || !p || !x0) return FDTD_ERR_NULL;
-  if (rows < 1 || C < 1) return FDTD_ERR_SIZE;
-  FNO_LAUNCH(fdtd::k_lift_fwd, fdtd::grid1((size_t)rows * C), 256, (size_t)rows, C, in, P, p, (bf16*)x0);
+  if (rows < 1 || C < 1 || cin < 1 || cin > fdtd::kLiftMaxIn) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_lift_fwd, fdtd::grid1((size_t)rows * C), 256, (size_t)rows, C, cin, in, P, p, (bf16*)x0);
 }
 
-int fno_lift_bwd(long long rows, int C, const float* in, const void* dx0, float* dP, float* dp,
+int fno_lift_bwd(long long rows, int C, int cin, const float* in, const void* dx0, float* dP, float* dp,
                  fdtd_stream_t stream) {
   if (!in || !dx0 || !dP || !dp) return FDTD_ERR_NULL;
-  if (rows < 1 || C < 1 || C > 65535) return FDTD_ERR_SIZE;
-  FNO_LAUNCH(fdtd::k_lift_bwd, dim3(64, C), 256, (size_t)rows, C, in, (const bf16*)dx0, dP, dp);
+  if (rows < 1 || C < 1 || C > 65535 || cin < 1 || cin > fdtd::kLiftMaxIn) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_lift_bwd, dim3(64, C), 256, (size_t)rows, C, cin, in, (const bf16*)dx0, dP, dp);
+}
+
+int fno_propagation(int n, int nbins, const float* feat, int nf, const double* wdt, double eps_scale,
+                    double sig_scale, double loss_scale, int probe_in, int probe_gap, float* P,
+                    fdtd_stream_t stream) {
+  if (!feat || !wdt || !P) return FDTD_ERR_NULL;
+  if (n < 1 || nbins < 1 || nf < 1 || nf > 64 || probe_in < 0 || probe_gap < 0 || !(eps_scale > 0))
+    return FDTD_ERR_SIZE;
+  const long long threads = 32LL * n;
+  FNO_LAUNCH(fdtd::k_propagation, dim3((unsigned)((threads + 255) / 256)), 256, n, nbins, feat, nf, wdt, eps_scale,
+             sig_scale, loss_scale, probe_in, probe_gap, P);
+}
+
+int fno_cmul(long long n, int nf, const float* P, const float* y, int conj_p, float* out, fdtd_stream_t stream) {
+  if (!P || !y || !out) return FDTD_ERR_NULL;
+  if (n < 1 || nf < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_cmul, fdtd::grid1((size_t)n * nf), 256, (size_t)n, nf, P, y, conj_p, out);
 }
 
 int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_t stream) {

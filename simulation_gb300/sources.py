@@ -17,7 +17,11 @@ import numpy as np
 def wave_values(wave: tuple, t_start: int, n: int) -> np.ndarray:
     """float64 values of ``wave`` for t = t_start .. t_start+n-1.
 
-    ``wave`` = ("gauss", t0, spread) | ("sin", ds, freq) | ("zero",).
+    ``wave`` = ("gauss", t0, spread) | ("dgauss", t0, spread) | ("sin", ds, freq)
+    | ("zero",).  "dgauss" is the derivative-of-Gaussian pulse -u exp(-u^2/2),
+    u = (t - t0)/spread (not a reference waveform): it carries no DC content,
+    so a soft source leaves no static charge whose slow decay in lossy layers
+    would outlast a finite run and bias its spectra.
     """
     out = np.zeros(n, dtype=np.float64)
     kind = wave[0]
@@ -25,6 +29,9 @@ def wave_values(wave: tuple, t_start: int, n: int) -> np.ndarray:
         t = t_start + k
         if kind == "gauss":
             out[k] = np.exp(-0.5 * ((t - wave[1]) / wave[2]) ** 2)
+        elif kind == "dgauss":
+            u = (t - wave[1]) / wave[2]
+            out[k] = -u * np.exp(-0.5 * u * u)
         elif kind == "sin":
             dt = wave[1] / 6e8
             out[k] = np.sin(2 * np.pi * wave[2] * dt * t)

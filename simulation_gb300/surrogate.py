@@ -3,20 +3,33 @@ to its transmission spectrum, trained and served on the GPU by the library's
 own BF16 tensor-core kernels, with batched FDTD as its judge and fallback.
 
 Network (no reference counterpart):
-* input:  (eps_r, sigma) of cells [0, 2*NBINS) of a slab run, averaged in
-  pairs to NBINS=2048 bins and scaled to [0, 1];
+* input:  cells [0, 2*NBINS) of a slab run as NBINS=2048 bins of 6 channels,
+  (eps_r-1)/8 and sigma/0.05 of cells 2b-1, 2b, 2b+1 (the whole profile, with
+  the interfaces between neighbouring bins visible inside one bin);
 * lift:   x0 = in P^T + p                                   [B, N, C=128]
 * 4 spectral layers, 32 retained modes:
     F  = x^T Phi^T        truncated real DFT (cos rows, -sin rows)
     G  = R_k F_k          complex 128x128 weights per mode
     x' = GELU(x W^T + Psi G^T + b)   (pointwise and inverse DFT share one
                                       tensor-core accumulator)
-* head:   o = H2 GELU(H1 mean_n(x) + hb1) + hb2              [B, 128] = (Re T, Im T) at 64 frequencies.
+* head:   y = H2 GELU(H1 mean_n(x) + hb1) + hb2              [B, 128]
+* frame:  T(f) = y(f) * P(f), P = exp(-i sum_cells k(f, cell)) the single-pass
+  propagation factor of the profile through the Yee update, computed in FP64
+  by ``fno_propagation``.  P carries the phase (thousands of radians across a
+  thick stack) and the attenuation (down to 1e-20) that BF16 activations
+  cannot hold; the network learns the rest: interface transmission, the
+  reflection seen at the entry probe and the multiple reflections.
 
 Every contraction runs in ``fdtd_gemm_bf16`` (tcgen05 tensor cores, FP32
 accumulation); every other op in the ``fno_*`` kernels.  Backward and Adam
 are hand-written too (``FNO.backward``, ``FNO.adam_step``).  Torch allocates
 device memory and gathers minibatches; it computes nothing of the network.
+
+Training data come from the batched FDTD kernel with a DC-free
+derivative-of-Gaussian soft source (``WAVE``): with the Gaussian pulse of the
+reference's programs the static charge left in lossy layers decays over far
+more than a run's 8000 steps and the DFT ratio of an opaque stack measures
+that tail, not the stack.
 """
 from __future__ import annotations
 
@@ -31,6 +44,8 @@ from . import batch1d as B1
 from .tc import gemm
 
 NBINS = 2048
+CIN = 6
+EPS_SCALE, SIG_SCALE = 8.0, 0.05
 WIDTH = 128
 MODES = 32
 LAYERS = 4
@@ -38,6 +53,10 @@ HIDDEN = 256
 NFREQ = 64
 OUT = 2 * NFREQ
 BF = torch.bfloat16
+FREQS = np.linspace(100e6, 3e9, NFREQ)
+WAVE = ("dgauss", 40, 6.0)
+NSTEPS = 8000
+PROBE_IN, PROBE_GAP = 30, 10  # entry probe cell; exit probe this far behind the stack
 
 
 def _st():
@@ -61,22 +80,43 @@ def dft_matrices(n: int = NBINS, m: int = MODES):
 
 
 def profile_features(batch: "B1.SlabBatch", idx=None, nbins: int = NBINS) -> np.ndarray:
-    """[n][nbins][2] float32 inputs: (eps_r-1)/8 and sigma/0.05 of cells
-    [0, 2*nbins), averaged in pairs (vacuum beyond a run's end)."""
+    """[n][nbins][6] float32 inputs: (eps_r-1)/8 of cells 2b-1, 2b, 2b+1, then
+    sigma/0.05 of the same cells (vacuum = 0, also beyond a run's end)."""
     idx = np.arange(batch.nruns) if idx is None else np.asarray(idx)
-    out = np.zeros((idx.size, nbins, 2), dtype=np.float32)
+    out = np.zeros((idx.size, nbins, CIN), dtype=np.float32)
     ncell = 2 * nbins
+    e = np.zeros(ncell + 2)  # e[c + 1] = cell c, padded with vacuum on both sides
+    s = np.zeros(ncell + 2)
     for q, r in enumerate(idx):
-        e = np.ones(ncell)
-        s = np.zeros(ncell)
+        e[:] = 0.0
+        s[:] = 0.0
         a, b = batch.layer_off[r], batch.layer_off[r + 1]
         for l in range(a, b):
             lo, hi = int(batch.layer_start[l]), min(int(batch.layer_end[l]), ncell)
             if lo < hi:
-                e[lo:hi] = batch.epsr[l]
-                s[lo:hi] = batch.sigma[l]
-        out[q, :, 0] = ((e.reshape(nbins, 2).mean(1)) - 1.0) / 8.0
-        out[q, :, 1] = s.reshape(nbins, 2).mean(1) / 0.05
+                e[lo + 1:hi + 1] = (batch.epsr[l] - 1.0) / EPS_SCALE
+                s[lo + 1:hi + 1] = batch.sigma[l] / SIG_SCALE
+        for j in range(3):  # cell 2b-1+j sits at e[2b+j]
+            out[q, :, j] = e[j:j + ncell:2]
+            out[q, :, 3 + j] = s[j:j + ncell:2]
+    return out
+
+
+def propagation(inp: torch.Tensor, freqs=FREQS, dt: float | None = None) -> torch.Tensor:
+    """[B][2*nf] float32 frame P of each profile (``fno_propagation``)."""
+    dt = B1.DT if dt is None else dt
+    wdt = torch.as_tensor(2 * np.pi * np.asarray(freqs, dtype=np.float64) * dt, device=inp.device)
+    nf = wdt.numel()
+    P = torch.empty((inp.shape[0], 2 * nf), dtype=torch.float32, device=inp.device)
+    _call("fno_propagation", inp.shape[0], inp.shape[1], inp.data_ptr(), nf, wdt.data_ptr(), EPS_SCALE, SIG_SCALE,
+          dt / (2 * B1.EPS0), PROBE_IN, PROBE_GAP, P.data_ptr())
+    return P
+
+
+def cmul(P: torch.Tensor, y: torch.Tensor, conj: bool = False) -> torch.Tensor:
+    """P (.) y (or conj(P) (.) y) for spectra stored [Re | Im]."""
+    out = torch.empty_like(y)
+    _call("fno_cmul", y.shape[0], y.shape[1] // 2, P.data_ptr(), y.data_ptr(), int(conj), out.data_ptr())
     return out
 
 
@@ -104,9 +144,10 @@ class FNO:
     """Parameters (FP32 master + BF16 copies) and the forward/backward kernels."""
 
     def __init__(self, seed: int = 0, device="cuda", nbins: int = NBINS, width: int = WIDTH, modes: int = MODES,
-                 layers: int = LAYERS, hidden: int = HIDDEN, out: int = OUT):
+                 layers: int = LAYERS, hidden: int = HIDDEN, out: int = OUT, cin: int = CIN):
         self.dev = torch.device(device)
         self.N, self.C, self.M, self.L, self.H, self.D = nbins, width, modes, layers, hidden, out
+        self.cin = cin
         g = torch.Generator().manual_seed(seed)
         C, M, H, D = width, modes, hidden, out
 
@@ -114,10 +155,9 @@ class FNO:
             return ((torch.rand(shape, generator=g, dtype=torch.float64) * 2 - 1) * scale).float().to(self.dev)
 
         self.p = {
-            "P": u(C, 2, scale=1.0), "pb": u(C, scale=0.5),
+            "P": u(C, cin, scale=1.0), "pb": u(C, scale=0.5),
             "H1": u(H, C, scale=1 / math.sqrt(C)), "hb1": u(H, scale=0.1),
-            # zero output layer: an untrained network predicts T = 0, the
-            # right answer for the many opaque stacks
+            # zero output layer: an untrained network predicts y = 0
             "H2": torch.zeros((D, H), device=self.dev), "hb2": torch.zeros(D, device=self.dev),
         }
         for l in range(layers):
@@ -158,11 +198,12 @@ class FNO:
 
     # ------------------------------------------------------------ forward
     def forward(self, inp: torch.Tensor, keep: bool = False) -> torch.Tensor:
-        """inp [B][N][2] float32 (device) -> out [B][D] float32."""
+        """inp [B][N][cin] float32 (device) -> network output y [B][D] float32."""
         Bn, N, C, M = inp.shape[0], self.N, self.C, self.M
         dev = self.dev
         x = torch.empty((Bn, N, C), dtype=BF, device=dev)
-        _call("fno_lift_fwd", Bn * N, C, inp.data_ptr(), self.p["P"].data_ptr(), self.p["pb"].data_ptr(), x.data_ptr())
+        _call("fno_lift_fwd", Bn * N, C, self.cin, inp.data_ptr(), self.p["P"].data_ptr(), self.p["pb"].data_ptr(),
+              x.data_ptr())
         saved = {"inp": inp, "x": [], "pre": [], "Fm": []}
         F = torch.empty((Bn, C, 2 * M), dtype=torch.float32, device=dev)
         Fm = torch.empty((M, Bn, 2 * C), dtype=BF, device=dev)
@@ -252,7 +293,7 @@ class FNO:
             dx32 = nd
         dx0 = torch.empty((Bn, N, C), dtype=BF, device=dev)
         _call("fno_to_bf16", dx32.numel(), dx32.data_ptr(), dx0.data_ptr())
-        _call("fno_lift_bwd", Bn * N, C, s["inp"].data_ptr(), dx0.data_ptr(), self.g["P"].data_ptr(),
+        _call("fno_lift_bwd", Bn * N, C, self.cin, s["inp"].data_ptr(), dx0.data_ptr(), self.g["P"].data_ptr(),
               self.g["pb"].data_ptr())
 
     def adam_step(self, lr: float = 1e-3, b1: float = 0.9, b2: float = 0.999, eps: float = 1e-8) -> None:
@@ -262,11 +303,14 @@ class FNO:
                   self.v[k].data_ptr(), lr, b1, b2, eps, self.step, None)
         self._refresh_bf16()
 
-    def loss_and_grad(self, inp: torch.Tensor, target: torch.Tensor, relative: bool = False) -> torch.Tensor:
-        """Forward, loss and backward.  ``relative`` uses the per-sample relative
-        squared error with the spectrum floor (the metric the judge applies);
-        otherwise the plain mean squared error."""
-        o = self.forward(inp, keep=True)
+    def loss_and_grad(self, inp: torch.Tensor, target: torch.Tensor, relative: bool = False,
+                      frame: torch.Tensor | None = None) -> torch.Tensor:
+        """Forward, loss and backward.  With ``frame`` P the loss is taken on
+        T = P (.) y (and dL/dy = conj(P) (.) dL/dT); ``relative`` uses the
+        per-sample relative squared error with the spectrum floor (the metric
+        the judge applies), otherwise the plain mean squared error."""
+        y = self.forward(inp, keep=True)
+        o = y if frame is None else cmul(frame, y)
         dO = torch.empty_like(o)
         loss = torch.zeros(1, dtype=torch.float32, device=self.dev)
         if relative:
@@ -276,42 +320,63 @@ class FNO:
         else:
             _call("fno_mse", o.shape[0], o.shape[1], o.data_ptr(), target.data_ptr(), dO.data_ptr(),
                   loss.data_ptr())
-        self.backward(dO)
+        self.backward(dO if frame is None else cmul(frame, dO, conj=True))
         return loss
 
     def predict(self, inp: torch.Tensor, chunk: int = 4096) -> torch.Tensor:
+        """Network output y for [B][N][cin] inputs, ``chunk`` profiles per pass."""
         outs = [self.forward(inp[i:i + chunk]) for i in range(0, inp.shape[0], chunk)]
+        return torch.cat(outs) if len(outs) > 1 else outs[0]
+
+    def spectrum(self, inp: torch.Tensor, chunk: int = 4096) -> torch.Tensor:
+        """Predicted transmission [B][2*NFREQ] = [Re T | Im T] = P (.) y."""
+        outs = []
+        for i in range(0, inp.shape[0], chunk):
+            part = inp[i:i + chunk]
+            outs.append(cmul(propagation(part), self.forward(part)))
         return torch.cat(outs) if len(outs) > 1 else outs[0]
 
 
 # ------------------------------------------------------------------ data and serving
-def generate_dataset(n: int, seed: int, nsteps: int = 8000, chunk: int = 4096, device="cuda"):
-    """Slab runs of the batched-FDTD distribution solved by the batched kernel:
-    returns (inputs [n][NBINS][2], targets [n][128], batch)."""
-    batch = B1.slab_batch(n, seed=seed)
-    targets = np.zeros((n, OUT), dtype=np.float32)
-    for s in range(0, n, chunk):
-        idx = np.arange(s, min(n, s + chunk))
-        r = B1.BatchRunner(batch.subset(idx), nsteps=nsteps, device=device)
+def solve_fdtd(batch: "B1.SlabBatch", nsteps: int = NSTEPS, chunk: int = 4096, device="cuda") -> np.ndarray:
+    """[n][128] transmission spectra of ``batch`` from the batched FDTD kernel."""
+    out = np.zeros((batch.nruns, OUT), dtype=np.float32)
+    for s in range(0, batch.nruns, chunk):
+        idx = np.arange(s, min(batch.nruns, s + chunk))
+        r = B1.BatchRunner(batch.subset(idx), nsteps=nsteps, freqs=FREQS, wave=WAVE, device=device)
         r.run()
-        targets[idx] = spectrum_targets(r.transmission())
-    return profile_features(batch), targets, batch
+        out[idx] = spectrum_targets(r.transmission())
+    return out
+
+
+def generate_dataset(n: int, seed: int, nsteps: int = NSTEPS, chunk: int = 4096, device="cuda"):
+    """Slab runs of the batched-FDTD distribution solved by the batched kernel:
+    returns (inputs [n][NBINS][6], targets [n][128], batch)."""
+    batch = B1.slab_batch(n, seed=seed)
+    if np.any(batch.probe_in != PROBE_IN) or np.any(batch.probe_out != batch.layer_end[batch.layer_off[1:] - 1]
+                                                    + PROBE_GAP):
+        raise ValueError("probe placement differs from the surrogate's frame")
+    return profile_features(batch), solve_fdtd(batch, nsteps, chunk, device), batch
 
 
 def train(model: FNO, inp: np.ndarray, tgt: np.ndarray, samples: int = 200_000, batch: int = 256,
-          lr: float = 1e-3, seed: int = 0, log_every: int = 100) -> list:
-    """Adam on random minibatches until ``samples`` samples have been seen."""
+          lr: float = 1e-3, lr_final: float = 1e-3, seed: int = 0, log_every: int = 100) -> list:
+    """Adam on random minibatches until ``samples`` samples have been seen; the
+    loss is the relative spectrum error of T = P (.) y.  The learning rate
+    follows a cosine from ``lr`` to ``lr_final``."""
     rng = np.random.default_rng(seed)
     dev = model.dev
     X = torch.as_tensor(inp).to(dev)
     Y = torch.as_tensor(tgt).to(dev)
+    frames = torch.cat([propagation(X[i:i + 65536]) for i in range(0, X.shape[0], 65536)])
     hist = []
     steps = max(1, samples // batch)
     for it in range(steps):
         idx = torch.as_tensor(rng.integers(0, X.shape[0], size=batch)).to(dev)
         loss = model.loss_and_grad(X.index_select(0, idx).contiguous(), Y.index_select(0, idx).contiguous(),
-                                   relative=True)
-        model.adam_step(lr)
+                                   relative=True, frame=frames.index_select(0, idx).contiguous())
+        a = 0.5 * (1 + math.cos(math.pi * it / max(1, steps - 1)))
+        model.adam_step(lr_final + (lr - lr_final) * a)
         if it % log_every == 0 or it == steps - 1:
             hist.append((it, float(loss.item())))
     return hist
@@ -322,20 +387,18 @@ class JudgedSurrogate:
     fraction of each request is re-solved by FDTD; a spot-checked profile whose
     error exceeds ``tol`` is replaced by its FDTD spectrum."""
 
-    def __init__(self, model: FNO, check_frac: float = 0.01, tol: float = 0.01, nsteps: int = 8000, seed: int = 0):
+    def __init__(self, model: FNO, check_frac: float = 0.01, tol: float = 0.01, nsteps: int = NSTEPS, seed: int = 0):
         self.model, self.check_frac, self.tol, self.nsteps = model, check_frac, tol, nsteps
         self.rng = np.random.default_rng(seed)
 
     def __call__(self, batch: "B1.SlabBatch", inp: torch.Tensor | None = None):
         if inp is None:
             inp = torch.as_tensor(profile_features(batch)).to(self.model.dev)
-        pred = self.model.predict(inp).cpu().numpy()
+        pred = self.model.spectrum(inp).cpu().numpy()
         n = batch.nruns
         k = max(1, int(round(self.check_frac * n)))
         idx = np.sort(self.rng.choice(n, size=k, replace=False))
-        r = B1.BatchRunner(batch.subset(idx), nsteps=self.nsteps, device=self.model.dev)
-        r.run()
-        ref = spectrum_targets(r.transmission())
+        ref = solve_fdtd(batch.subset(idx), self.nsteps, device=self.model.dev)
         err = rel_l2_spectrum(pred[idx], ref)
         bad = err > self.tol
         pred[idx[bad]] = ref[bad]
@@ -344,14 +407,28 @@ class JudgedSurrogate:
                       "checked_idx": idx}
 
 
-def time_inference(model: FNO, n: int = 65536, chunk: int = 4096, reps: int = 2) -> float:
-    """Spectra per second of the network alone at batch ``n`` (synthetic inputs)."""
-    inp = torch.rand((chunk, model.N, 2), device=model.dev)
-    model.forward(inp)
+def time_inference(model: FNO, n: int = 65536, chunk: int = 4096, reps: int = 2, seed: int = 0) -> float:
+    """Spectra per second of the served path (network, frame and product) at
+    batch ``n``, timed with CUDA events on the current stream.  Inputs are
+    ``chunk`` seeded slab profiles reused for every chunk: the network's cost
+    does not depend on the values; the frame's grows with the number of
+    material changes along a profile (a few per layered stack)."""
+    inp = torch.as_tensor(profile_features(B1.slab_batch(chunk, seed=seed), nbins=model.N)).to(model.dev)
+    model.spectrum(inp)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    t0 = time.perf_counter()
+    e0.record(st)
     for _ in range(reps):
         for _ in range(0, n, chunk):
-            model.forward(inp)
+            model.spectrum(inp)
+    e1.record(st)
     torch.cuda.synchronize()
-    return reps * n / (time.perf_counter() - t0)
+    return reps * n / (e0.elapsed_time(e1) / 1e3)
+
+
+def flops_per_sample(model: FNO) -> float:
+    """Tensor-core FLOPs of one forward pass (the GEMMs)."""
+    N, C, M, H, D = model.N, model.C, model.M, model.H, model.D
+    per_layer = 2 * N * C * 2 * M + 2 * M * (2 * C) * (2 * C) + 2 * N * C * (C + 2 * M)
+    return model.L * per_layer + 2 * C * H + 2 * H * D

@@ -1,6 +1,8 @@
 """The neural-operator surrogate on the GPU: forward and gradients of the
-hand-written BF16 kernels against the FP64 CPU oracle, training that lowers
-the loss, and the FDTD judge/fallback."""
+hand-written BF16 kernels against the FP64 CPU oracle (plain and in the
+propagation frame with the relative loss), the frame kernel against its FP64
+oracle, converged FDTD training targets, training that lowers the loss, and
+the FDTD judge/fallback."""
 import numpy as np
 import pytest
 import torch
@@ -13,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 def _small_model():
     from simulation_gb300 import surrogate as S
-    return S.FNO(seed=1, nbins=256, width=128, modes=16, layers=2, hidden=256, out=128)
+    return S.FNO(seed=1, nbins=256, width=128, modes=16, layers=2, hidden=256, out=128, cin=6)
 
 
 def test_forward_and_gradients_vs_fp64_oracle(cuda_lib):
@@ -23,7 +25,7 @@ def test_forward_and_gradients_vs_fp64_oracle(cuda_lib):
     m.p["H2"].copy_(((torch.rand(m.p["H2"].shape, generator=g) * 2 - 1) / 16).cuda())
     m.p["hb2"].copy_(((torch.rand(m.p["hb2"].shape, generator=g) * 2 - 1) / 10).cuda())
     m._refresh_bf16()
-    inp = torch.rand((8, 256, 2), generator=g)
+    inp = torch.rand((8, 256, 6), generator=g)
     tgt = torch.randn((8, 128), generator=g) * 0.3
     loss = m.loss_and_grad(inp.cuda(), tgt.cuda())
     o_gpu = m._saved  # noqa: F841  (kept alive until here)
@@ -40,11 +42,89 @@ def test_forward_and_gradients_vs_fp64_oracle(cuda_lib):
     assert not bad, f"gradient rel-L2 above 6e-2: {bad}"
 
 
+def test_gradients_in_frame_with_relative_loss(cuda_lib):
+    """loss on T = P (.) y, per-sample relative with the spectrum floor."""
+    from simulation_gb300 import surrogate as S
+    m = _small_model()
+    g = torch.Generator().manual_seed(3)
+    m.p["H2"].copy_(((torch.rand(m.p["H2"].shape, generator=g) * 2 - 1) / 16).cuda())
+    m.p["hb2"].copy_(((torch.rand(m.p["hb2"].shape, generator=g) * 2 - 1) / 10).cuda())
+    m._refresh_bf16()
+    inp = torch.rand((8, 256, 6), generator=g)
+    ph = torch.rand((8, 64), generator=g) * 6.283
+    amp = 10.0 ** (-4 * torch.rand((8, 1), generator=g))  # frames from 1 down to 1e-4
+    frame = torch.cat([amp * torch.cos(ph), -amp * torch.sin(ph)], dim=1)
+    tgt = torch.randn((8, 128), generator=g) * 0.3 * amp
+    loss = m.loss_and_grad(inp.cuda(), tgt.cuda(), relative=True, frame=frame.cuda())
+    torch.cuda.synchronize()
+    floor2 = S.SPECTRUM_FLOOR ** 2 * 64
+    params = {k: v.detach().cpu() for k, v in m.p.items()}
+    l_ref, _, g_ref = fno_ref.loss_and_grads(params, inp, tgt, layers=2, modes=16, frame=frame, rel_floor2=floor2)
+    assert abs(float(loss.item()) - l_ref) <= 3e-2 * l_ref
+    bad = {}
+    for k, gr in g_ref.items():
+        e = rel_l2(m.g[k].cpu().double().numpy(), gr.numpy())
+        if e > 6e-2:
+            bad[k] = e
+    assert not bad, f"gradient rel-L2 above 6e-2: {bad}"
+
+
+def test_cmul_matches_complex_product(cuda_lib):
+    from simulation_gb300 import surrogate as S
+    g = torch.Generator().manual_seed(4)
+    P = torch.randn((5, 128), generator=g)
+    y = torch.randn((5, 128), generator=g)
+    Pc = (P[:, :64] + 1j * P[:, 64:]).numpy()
+    yc = (y[:, :64] + 1j * y[:, 64:]).numpy()
+    for conj, ref in [(False, Pc * yc), (True, np.conj(Pc) * yc)]:
+        out = S.cmul(P.cuda(), y.cuda(), conj=conj).cpu().numpy()
+        np.testing.assert_allclose(out[:, :64] + 1j * out[:, 64:], ref, rtol=1e-5, atol=1e-6)
+
+
+def test_propagation_frame_vs_fp64_oracle(cuda_lib):
+    """``fno_propagation`` (FP64 on the device, from the features alone) against
+    the NumPy restatement: |P| spans 1 .. 1e-30, phases thousands of radians."""
+    from oracle import slab_spectrum as SS
+    from simulation_gb300 import batch1d as B1
+    from simulation_gb300 import surrogate as S
+    batch = B1.slab_batch(48, seed=21)
+    feat = S.profile_features(batch)
+    P = S.propagation(torch.as_tensor(feat).cuda()).cpu().numpy().astype(np.float64)
+    Pg = P[:, :64] + 1j * P[:, 64:]
+    for r in range(batch.nruns):
+        ref = SS.propagation_from_features(feat[r], S.FREQS, B1.DT, S.PROBE_IN, S.PROBE_GAP)
+        ok = np.abs(ref) > 1e-30
+        np.testing.assert_allclose(Pg[r, ok], ref[ok], rtol=2e-5, err_msg=f"run {r}")
+
+
+def test_fdtd_targets_are_converged(cuda_lib):
+    """The batched kernel with the surrogate's DC-free pulse and 8000 steps
+    gives the steady-state transmission of the frequency-domain oracle."""
+    from oracle import slab_spectrum as SS
+    from simulation_gb300 import batch1d as B1
+    from simulation_gb300 import surrogate as S
+    batch = B1.slab_batch(64, seed=22)
+    T = S.solve_fdtd(batch)
+    floor = S.SPECTRUM_FLOOR * np.sqrt(64)
+    errs = []
+    for r in range(batch.nruns):
+        a, b = batch.layer_off[r], batch.layer_off[r + 1]
+        ca, cb = SS.cell_coeffs(int(batch.ke[r]), batch.layer_start[a:b], batch.layer_end[a:b], batch.epsr[a:b],
+                                batch.sigma[a:b], B1.DT, np.float32)
+        Ts = SS.steady_transmission(ca, cb, int(batch.probe_in[r]), int(batch.probe_out[r]), S.FREQS, B1.DT)
+        ref = np.concatenate([Ts.real, Ts.imag])
+        errs.append(np.linalg.norm(T[r] - ref) / max(np.linalg.norm(ref), floor))
+    # a few low-loss, high-contrast stacks still ring at step 8000 (their
+    # echo train decays by |r|^2 per round trip): bounded, not converged
+    errs = np.array(errs)
+    assert np.median(errs) <= 1e-3 and np.quantile(errs, 0.9) <= 5e-3 and errs.max() <= 3e-2, errs
+
+
 def test_training_lowers_loss(cuda_lib):
     m = _small_model()
     g = torch.Generator().manual_seed(2)
-    X = torch.rand((64, 256, 2), generator=g).cuda()
-    W = torch.randn((2, 128), generator=g).cuda()
+    X = torch.rand((64, 256, 6), generator=g).cuda()
+    W = torch.randn((6, 128), generator=g).cuda()
     Y = torch.tanh(X.mean(1) @ W).contiguous()  # a smooth function of the profile
     first = float(m.loss_and_grad(X, Y).item())
     for _ in range(60):
@@ -60,13 +140,48 @@ def test_judge_replaces_bad_predictions(cuda_lib):
     from simulation_gb300 import batch1d as B1
     from simulation_gb300 import surrogate as S
     m = S.FNO(seed=0)
-    m.p["hb2"].fill_(0.05)  # a deliberately wrong network
+    m.p["hb2"].fill_(3.0)  # a deliberately wrong network: y = 3 + 3i everywhere
     m._refresh_bf16()
-    batch = B1.slab_batch(200, seed=4)
-    judge = S.JudgedSurrogate(m, check_frac=0.05, tol=0.01, nsteps=2000, seed=0)
+    batch = B1.slab_batch(400, seed=4)
+    judge = S.JudgedSurrogate(m, check_frac=0.1, tol=0.01, nsteps=2000, seed=0)
     pred, info = judge(batch)
-    assert info["checked"] == 10 and info["fell_back"] == 10
-    r = B1.BatchRunner(batch.subset(info["checked_idx"]), nsteps=2000)
-    r.run()
-    ref = S.spectrum_targets(r.transmission())
+    assert info["checked"] == 40 and info["fell_back"] >= 1
+    ref = S.solve_fdtd(batch.subset(info["checked_idx"]), nsteps=2000)
     assert np.all(S.rel_l2_spectrum(pred[info["checked_idx"]], ref) <= 0.01)
+
+
+def test_trained_network_gains_over_baselines_and_fdtd(cuda_lib):
+    """What the learned part adds: after a short training on batched-FDTD
+    data, held-out spectra are closer than both the zero spectrum and the bare
+    propagation frame (y = 1), and the served path delivers spectra far faster
+    than the batched FDTD that produced them."""
+    from simulation_gb300 import batch1d as B1
+    from simulation_gb300 import surrogate as S
+    ntr = 12288
+    X, Y, _ = S.generate_dataset(ntr + 1024, seed=31)
+    m = S.FNO(seed=0)
+    S.train(m, X[:ntr], Y[:ntr], samples=160_000, batch=256, lr=1e-3, lr_final=1e-4)
+    Yte = Y[ntr:]
+    Xd = torch.as_tensor(X[ntr:]).cuda()
+    e_net = S.rel_l2_spectrum(m.spectrum(Xd).cpu().numpy(), Yte)
+    P = S.propagation(Xd)
+    ones = torch.zeros_like(P)
+    ones[:, :S.NFREQ] = 1.0
+    e_frame = S.rel_l2_spectrum(S.cmul(P, ones).cpu().numpy(), Yte)
+    e_zero = S.rel_l2_spectrum(np.zeros_like(Yte), Yte)
+    big = np.linalg.norm(Yte, axis=1) > S.SPECTRUM_FLOOR * np.sqrt(S.NFREQ)
+    assert big.sum() >= 50
+    assert np.mean(e_net <= 0.01) >= np.mean(e_zero <= 0.01) + 0.05, (np.mean(e_net <= 0.01), np.mean(e_zero <= 0.01))
+    assert np.median(e_net[big]) <= 0.3 * np.median(e_frame[big]), (np.median(e_net[big]), np.median(e_frame[big]))
+    # throughput of the served path against the batched FDTD (default tuning) on the same distribution
+    sps = S.time_inference(m, n=16384, chunk=4096, reps=1)
+    r = B1.BatchRunner(B1.slab_batch(4096, seed=32), nsteps=S.NSTEPS, freqs=S.FREQS, wave=S.WAVE)
+    r.run()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    r.run()
+    e1.record()
+    torch.cuda.synchronize()
+    fdtd_sps = 4096 / (e0.elapsed_time(e1) / 1e3)
+    assert sps >= 20 * fdtd_sps, (sps, fdtd_sps)
