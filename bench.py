@@ -370,7 +370,17 @@ def _bench_adjoint(st) -> dict:
     return res
 
 
-def _bench_surrogate(st, fdtd_spectra_per_s: float) -> dict:
+def run_only(args) -> None:
+    import torch
+    st = torch.cuda.current_stream()
+    if args.only == "adjoint":
+        res = _bench_adjoint(st)
+    else:
+        res = _bench_surrogate(st, None, n=args.batch)
+    print(json.dumps({"workload": args.only, **res}), flush=True)
+
+
+def _bench_surrogate(st, fdtd_spectra_per_s: float | None, n: int = 65536) -> dict:
     """Served surrogate (network, propagation frame, product) at batch 65536;
     throughput does not depend on the weights, so a seeded untrained network
     is timed.  Tensor-core FLOPs against the measured dense BF16 peak."""
@@ -378,12 +388,12 @@ def _bench_surrogate(st, fdtd_spectra_per_s: float) -> dict:
 
     from simulation_gb300 import surrogate as S
     m = S.FNO(seed=0)
-    sps = S.time_inference(m, n=65536, chunk=4096, reps=1)
+    sps = S.time_inference(m, n=n, chunk=min(n, 4096), reps=1)
     fl = S.flops_per_sample(m)
     peak = _peaks_bf16()
     res = {"spectra_per_s": sps, "gflop_per_sample": fl / 1e9, "tflops": sps * fl / 1e12,
            "frac_of_bf16_peak": None if peak is None else sps * fl / 1e12 / peak,
-           "vs_batched_fdtd_spectra_per_s": sps / fdtd_spectra_per_s}
+           "vs_batched_fdtd_spectra_per_s": None if not fdtd_spectra_per_s else sps / fdtd_spectra_per_s}
     del m
     torch.cuda.empty_cache()
     return res
@@ -437,7 +447,13 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
+    ap.add_argument("--only", choices=["surrogate", "adjoint"],
+                    help="run one secondary workload alone and print its JSON (profiling runs)")
+    ap.add_argument("--batch", type=int, default=65536, help="surrogate spectra per timed pass (--only surrogate)")
     args = ap.parse_args()
+    if args.only:
+        run_only(args)
+        return
     global NX, NY, NS
     NX = NY = args.grid
     NS = args.ns

@@ -92,8 +92,14 @@ __device__ __forceinline__ bool all_finite(const float (&v)[CPL]) {
   return ok;
 }
 
-template <int K, int CPL, bool LOSSY, bool PML, int WARPS>
-__global__ void __launch_bounds__(WARPS * 32) k_march(const MarchArgs a) {
+// The Ez probe (the adjoint's objective trace) is a separate instantiation,
+// so the benchmark kernels carry no per-cell probe test.  Kernels with
+// 64-column stripes are held to four 4-warp blocks per SM (128 registers, no
+// spills); left free, the compiler takes 138-142 registers and the SM runs
+// three blocks (-9% to -20% at 8192^2, K = 4).  128-column stripes need more
+// registers and are left free.
+template <int K, int CPL, bool LOSSY, bool PML, int WARPS, bool PROBE>
+__global__ void __launch_bounds__(WARPS * 32, CPL == 2 ? 4 : 1) k_march(const MarchArgs a) {
   constexpr int W = 32 * CPL;
   constexpr int OUTW = W - 2 * HALO;
   static_assert(K >= 1 && K <= HALO, "steps per pass must not exceed the halo");
@@ -207,8 +213,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_march(const MarchArgs a) {
         ne[c] = e;
         // the probe cell's Ez is recorded by the warp that owns it (output
         // column, row inside the segment), where every level is valid
-        if (a.probe_ez && q == a.probe_i && j == a.probe_j && vout && q >= i_s && q < i_e)
-          a.probe_ez[a.t0 + s] = e;
+        if (PROBE && q == a.probe_i && j == a.probe_j && vout && q >= i_s && q < i_e) a.probe_ez[a.t0 + s] = e;
       }
 
       // ---- H on row qc (needs Ez of rows qc and q at this level)
@@ -292,14 +297,19 @@ struct MarchConfig {
 
 MarchConfig g_cfg;  // tuning knob (fdtd2d_set_march_config)
 
-template <int K, int CPL, bool LOSSY, bool PML>
+// Shortest automatic segment: 4K rows (the recomputed cone is 2K), at least 8.
+// Measured at 1024^2 (adjoint forward/recompute): 8 rows for K <= 2 and 16 for
+// K = 4 beat 16/32 by 1.3-2x, because small grids otherwise leave most SMs idle.
+constexpr int min_seg_rows(int K) { return K * 4 > 8 ? K * 4 : 8; }
+
+template <int K, int CPL, bool LOSSY, bool PML, bool PROBE>
 int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
   constexpr int WARPS = 4;
   (void)warps_cfg;
   MarchArgs a = a0;
   constexpr int W = 32 * CPL;
   constexpr int OUTW = W - 2 * HALO;
-  auto kern = k_march<K, CPL, LOSSY, PML, WARPS>;
+  auto kern = k_march<K, CPL, LOSSY, PML, WARPS, PROBE>;
   const size_t smem = PML ? (size_t)WARPS * 5 * W * sizeof(float) : 0;
   a.n_stripes = (a.ny + OUTW - 1) / OUTW;
   int seg_rows = seg_cfg;
@@ -315,7 +325,7 @@ int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
     if (n_segs < 1) n_segs = 1;
     seg_rows = (int)((a.nx + n_segs - 1) / n_segs);
     // keep the recomputed cone (2K rows per segment) small
-    seg_rows = std::max(seg_rows, 16 * K);
+    seg_rows = std::max(seg_rows, min_seg_rows(K));
   }
   a.seg_rows = seg_rows;
   a.n_segs = (a.nx + seg_rows - 1) / seg_rows;
@@ -327,10 +337,16 @@ int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
 
 template <int K, int CPL>
 int launch_k(const MarchArgs& a, bool lossy, bool pml, cudaStream_t st) {
-  if (lossy && pml) return launch_t<K, CPL, true, true>(a, g_cfg.warps, g_cfg.seg_rows, st);
-  if (lossy) return launch_t<K, CPL, true, false>(a, g_cfg.warps, g_cfg.seg_rows, st);
-  if (pml) return launch_t<K, CPL, false, true>(a, g_cfg.warps, g_cfg.seg_rows, st);
-  return launch_t<K, CPL, false, false>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  if (a.probe_ez) {
+    if (lossy && pml) return launch_t<K, CPL, true, true, true>(a, g_cfg.warps, g_cfg.seg_rows, st);
+    if (lossy) return launch_t<K, CPL, true, false, true>(a, g_cfg.warps, g_cfg.seg_rows, st);
+    if (pml) return launch_t<K, CPL, false, true, true>(a, g_cfg.warps, g_cfg.seg_rows, st);
+    return launch_t<K, CPL, false, false, true>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  }
+  if (lossy && pml) return launch_t<K, CPL, true, true, false>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  if (lossy) return launch_t<K, CPL, true, false, false>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  if (pml) return launch_t<K, CPL, false, true, false>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  return launch_t<K, CPL, false, false, false>(a, g_cfg.warps, g_cfg.seg_rows, st);
 }
 
 template <int CPL>
@@ -371,7 +387,17 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
   a.probe_ez = probe_ez;
   const bool lossy = p.nbz != nullptr;
   const bool pml = has_pml(p);
-  const int cpl = g_cfg.cpl ? g_cfg.cpl : (k >= 3 ? 2 : 4);
+  int cpl = g_cfg.cpl ? g_cfg.cpl : (k >= 3 ? 2 : 4);
+  if (!g_cfg.cpl && cpl == 4 && k >= 1 && k <= HALO) {
+    // small grids: if 128-column stripes times the shortest segments would not
+    // fill one wave of warps (32 per SM), use 64-column stripes instead
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const long stripes = (p.ny + (32 * 4 - 2 * HALO) - 1) / (32 * 4 - 2 * HALO);
+    const long segs = (p.nx + min_seg_rows(k) - 1) / min_seg_rows(k);
+    if (stripes * segs < 32L * nsm) cpl = 2;
+  }
   if (cpl == 2) return launch_cpl<2>(a, k, lossy, pml, st);
   return launch_cpl<4>(a, k, lossy, pml, st);
 }

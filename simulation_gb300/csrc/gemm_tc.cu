@@ -4,17 +4,20 @@
 // (truncated DFT, inverse DFT, channel mixing, pointwise layers and their
 // gradients).
 //
-// 128 x BN output tiles, persistent CTAs of 6 warps:
-//   * warp 4, one lane: TMA producer.  Each pipeline stage holds a 128 x 64
+// 128 x BN output tiles, persistent CTAs of 10 warps:
+//   * warp 8, one lane: TMA producer.  Each pipeline stage holds a 128 x 64
 //     A tile and a BN x 64 B tile in 128-byte-swizzled shared memory, loaded
 //     by cp.async.bulk.tensor with mbarrier completion;
-//   * warp 5, one lane: issues tcgen05.mma (kind::f16, BF16 inputs, FP32
+//   * warp 9, one lane: issues tcgen05.mma (kind::f16, BF16 inputs, FP32
 //     accumulator in TMEM), four 16-deep MMAs per stage, and tcgen05.commit
 //     to release the stage and, per tile, to signal the epilogue;
-//   * warps 0-3: read the accumulator with tcgen05.ld (warp w owns TMEM lanes
-//     32w..32w+31 = output rows), return the TMEM buffer, apply the epilogue
-//     and store; two accumulator buffers overlap a tile's epilogue with the
-//     next tile's MMAs.
+//   * warps 0-7: read the accumulator with tcgen05.ld (warp w owns TMEM lanes
+//     32(w%4)..32(w%4)+31 = output rows, and half w/4 of the columns), return
+//     the TMEM buffer, apply the epilogue and store; two accumulator buffers
+//     overlap a tile's epilogue with the next tile's MMAs.  Eight epilogue
+//     warps (two per SM sub-partition) rather than four: with four, the
+//     pointwise layer's GEMM (K = 192) spent most of its time in the
+//     epilogue and moved 3.6 TB/s.
 // Operands may be K-major or MN-major (the transposed products of the
 // backward pass need MN-major), selected per call.  Every wait on an mbarrier
 // is bounded (about 2 s): on expiry the kernel records FDTD_STATUS_TIMEOUT in
@@ -33,7 +36,7 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BK = 64;      // one 128-byte swizzle atom of BF16 along K
-constexpr int EPI_WARPS = 4;
+constexpr int EPI_WARPS = 8;
 constexpr int THREADS = 32 * (EPI_WARPS + 2);
 
 struct GemmArgs {
@@ -127,8 +130,8 @@ __device__ __forceinline__ float gelu(float z) {
   return 0.5f * z * (1.0f + tanh_hw(u));
 }
 
-// Persistent, warp-specialised kernel: warps 0-3 drain accumulators
-// (epilogue), warp 4 is the TMA producer, warp 5 issues the MMAs.  Two TMEM
+// Persistent, warp-specialised kernel: warps 0-7 drain accumulators
+// (epilogue), warp 8 is the TMA producer, warp 9 issues the MMAs.  Two TMEM
 // accumulator buffers let the epilogue of one tile overlap the MMAs of the
 // next; tiles are taken round-robin (tile = blockIdx.x + i * gridDim.x, M tiles
 // fastest so neighbouring CTAs share B tiles in L2).
@@ -264,7 +267,9 @@ __global__ void __launch_bounds__(THREADS, 1)
       }
     }
   } else {
-    // ------------------------------------------------ epilogue warps 0-3
+    // ------------------------------------------------ epilogue warps 0-7
+    const int lg = warp & 3;                       // TMEM lane group = 32 output rows
+    const int c_begin = (warp >> 2) * (BN / 2), c_end = c_begin + BN / 2;
     int i = 0;
     for (long long t = blockIdx.x; t < total; t += gridDim.x, ++i) {
       const int bz = (int)(t / ((long long)mt * nt));
@@ -275,13 +280,13 @@ __global__ void __launch_bounds__(THREADS, 1)
           __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull[b]), (uint32_t)((i >> 1) & 1), a.status));
       if (!have) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int row = m0 + warp * 32 + lane;
+      const int row = m0 + lg * 32 + lane;
       const size_t cbase = (size_t)bz * a.stride_c + (size_t)row * a.ldc;
       const size_t rbase = (size_t)bz * a.stride_r + (size_t)row * a.ldr;
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = c_begin; c0 < c_end; c0 += 32) {
         uint32_t r[32];
-        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * BN + c0);
+        const uint32_t taddr = tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)(b * BN + c0);
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
             "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -293,8 +298,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             : "r"(taddr)
             : "memory");
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (c0 + 32 >= BN) {
-          // the whole accumulator has been read: hand the TMEM buffer back
+        if (c0 + 32 >= c_end) {
+          // this warp's part of the accumulator has been read: release it
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
           if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&tempty[b])) : "memory");
