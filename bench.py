@@ -300,48 +300,56 @@ def run_ours(args) -> None:
 
 def run_secondary(args, st, world) -> dict:
     """The other workloads of the path, measured after the headline (not part of `value`)."""
-    import numpy as np
+    import torch
+    out = {"fd1d_dielectric_ke200_1000steps": _bench_fd1d(st)}
+    batch = _bench_batch1d(st)
+    out["batch1d_4096_slabs_8000steps"] = batch
+    out["adjoint_1024sq_3000steps"] = _bench_adjoint(st)
+    out["surrogate_fno_batch65536"] = _bench_surrogate(st, batch["spectra_per_s"])
+    torch.cuda.empty_cache()
+    return out
+
+
+def _bench_fd1d(st, reps: int = 20) -> dict:
+    """Plain 1D dielectric case: ke=200, hard source at k=5, 1000 steps, one fused launch."""
     import torch
 
-    from simulation_gb300 import batch1d as B
     from simulation_gb300 import fd1d as G1
-    out = {}
-    # plain 1D dielectric case: ke=200, hard source at k=5, 1000 steps, one fused launch
     sim = G1.program("config1", ns=1000)
     for _ in range(5):
         sim.t = 0
         sim.step(1000)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
-    for _ in range(20):
+    for _ in range(reps):
         sim.t = 0
         sim.step(1000)
     e1.record(st)
     torch.cuda.synchronize()
-    us = e0.elapsed_time(e1) * 1e3 / 20
-    out["fd1d_dielectric_ke200_1000steps"] = {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3,
-                                              "kernel_launches_per_run": 1}
-    # batched uneven 1D slab runs: 4096 runs, ke ~ U[500,20000], 8000 steps, 64-frequency probes
-    batch = B.slab_batch(4096, seed=0)
+    us = e0.elapsed_time(e1) * 1e3 / reps
+    return {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3, "kernel_launches_per_run": 1}
+
+
+def _bench_batch1d(st, nruns: int = 4096, autotune: bool = True) -> dict:
+    """Batched uneven 1D slab runs: ke ~ U[500,20000], 8000 steps, 64-frequency probes."""
+    import torch
+
+    from simulation_gb300 import batch1d as B
+    batch = B.slab_batch(nruns, seed=0)
     runner = B.BatchRunner(batch, nsteps=8000)
-    tuned = B.autotune(runner, probe_steps=400, reps=1)
+    tuned = B.autotune(runner, probe_steps=400, reps=1) if autotune else {"tuning": runner.tuning}
     runner.run()
     torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
     runner.run()
     e1.record(st)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     cells = int(batch.ke.sum()) * 8000
-    out["batch1d_4096_slabs_8000steps"] = {"ms": ms, "Gcell_updates_per_s": cells / ms / 1e6,
-                                           "spectra_per_s": batch.nruns / ms * 1e3, "tuning": tuned["tuning"],
-                                           "status": int(runner.status.item()),
-                                           "runs_done": int(runner.done.sum().item())}
-    del runner
-    out["adjoint_1024sq_3000steps"] = _bench_adjoint(st)
-    out["surrogate_fno_batch65536"] = _bench_surrogate(st, batch.nruns / ms * 1e3)
-    torch.cuda.empty_cache()
-    return out
+    return {"ms": ms, "Gcell_updates_per_s": cells / ms / 1e6, "spectra_per_s": batch.nruns / ms * 1e3,
+            "tuning": tuned["tuning"], "status": int(runner.status.item()),
+            "runs_done": int(runner.done.sum().item())}
 
 
 def _bench_adjoint(st) -> dict:
@@ -375,6 +383,10 @@ def run_only(args) -> None:
     st = torch.cuda.current_stream()
     if args.only == "adjoint":
         res = _bench_adjoint(st)
+    elif args.only == "batch1d":
+        res = _bench_batch1d(st, nruns=args.batch if args.batch != 65536 else 4096, autotune=False)
+    elif args.only == "fd1d":
+        res = _bench_fd1d(st, reps=5)
     else:
         res = _bench_surrogate(st, None, n=args.batch)
     print(json.dumps({"workload": args.only, **res}), flush=True)
@@ -447,9 +459,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
-    ap.add_argument("--only", choices=["surrogate", "adjoint"],
+    ap.add_argument("--only", choices=["surrogate", "adjoint", "batch1d", "fd1d"],
                     help="run one secondary workload alone and print its JSON (profiling runs)")
-    ap.add_argument("--batch", type=int, default=65536, help="surrogate spectra per timed pass (--only surrogate)")
+    ap.add_argument("--batch", type=int, default=65536,
+                    help="surrogate spectra per timed pass (--only surrogate); runs for --only batch1d (default 4096)")
     args = ap.parse_args()
     if args.only:
         run_only(args)
