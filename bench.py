@@ -304,9 +304,37 @@ def run_secondary(args, st, world) -> dict:
     out = {"fd1d_dielectric_ke200_1000steps": _bench_fd1d(st)}
     batch = _bench_batch1d(st)
     out["batch1d_4096_slabs_8000steps"] = batch
+    out["fd2d_tfsf_dft_2048sq"] = _bench_tfsf_dft(st)
     out["adjoint_1024sq_3000steps"] = _bench_adjoint(st)
     out["surrogate_fno_batch65536"] = _bench_surrogate(st, batch["spectra_per_s"])
     torch.cuda.empty_cache()
+    return out
+
+
+def _bench_tfsf_dft(st, n: int = 2048, steps: int = 400) -> dict:
+    """The fd2d_3_4 program (TF/SF plane wave, lossy cylinder, PML, 3-frequency
+    full-field DFT) at n^2: one step is three launches (fdtd2d_step_n), timed
+    beside the nine per-function launches of the reference's loop."""
+    import torch
+
+    from simulation_gb300 import fd2d as G
+    dt = 0.01 / 6e8
+    naz, nbz = G.dielectric(n, n, 32, n // 8, dt, 30.0, 0.30)
+    sim = G.SimTM2D(n, n, pml=G.pmlparam(n, n, 32), naz=naz, nbz=nbz, lossy=True, tfsf_npml=32,
+                    freq=[50e6, 300e6, 700e6], dt=dt, ns=3 * steps)
+    out = {}
+    for name, fn in (("three_launch", sim.step), ("per_function", sim.step_per_function)):
+        fn(20)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        fn(steps)
+        e1.record(st)
+        torch.cuda.synchronize()
+        out[f"{name}_Gcell_updates_per_s"] = n * n * steps / (e0.elapsed_time(e1) / 1e3) / 1e9
+    out["grid"] = [n, n]
+    out["launches_per_step"] = {"three_launch": 3, "per_function": 9}
+    del sim
     return out
 
 
@@ -387,6 +415,8 @@ def run_only(args) -> None:
         res = _bench_batch1d(st, nruns=args.batch if args.batch != 65536 else 4096, autotune=False)
     elif args.only == "fd1d":
         res = _bench_fd1d(st, reps=5)
+    elif args.only == "tfsf":
+        res = _bench_tfsf_dft(st)
     else:
         res = _bench_surrogate(st, None, n=args.batch)
     print(json.dumps({"workload": args.only, **res}), flush=True)
@@ -459,7 +489,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the secondary workloads")
-    ap.add_argument("--only", choices=["surrogate", "adjoint", "batch1d", "fd1d"],
+    ap.add_argument("--only", choices=["surrogate", "adjoint", "batch1d", "fd1d", "tfsf"],
                     help="run one secondary workload alone and print its JSON (profiling runs)")
     ap.add_argument("--batch", type=int, default=65536,
                     help="surrogate spectra per timed pass (--only surrogate); runs for --only batch1d (default 4096)")

@@ -67,15 +67,12 @@ size_t slot_bytes(const fdtd2d_params* p) {
 
 int nslots(const fdtd2d_params* p) { return 3 + (p->nbz ? 1 : 0) + (has_pml(*p) ? 2 : 0); }
 
-// one time step with the per-function kernels, in the reference's order
-// (fd2d/python/fd2d_3_4.py:268-277)
-int step_per_function(int t, const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st) {
+// one time step in the reference's order (fd2d/python/fd2d_3_4.py:268-277):
+// ezinct, dfield, inctdz, efield, fourier, hxinct, hfield, incthx, incthy in
+// three launches (launch_step3), bitwise equal to the nine functions
+int step_three_launches(int t, const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st) {
   int rc;
-  const bool tfsf = p.tfsf_npml > 0;
-  if (tfsf && (rc = launch_ezinct(p, s, st))) return rc;
-  if ((rc = launch_dfield(t, p, s, st))) return rc;
-  if (tfsf && (rc = launch_inctdz(p, s, st))) return rc;
-  if ((rc = launch_efield(p, s, st))) return rc;
+  if ((rc = launch_step3(t, p, s, st))) return rc;
   if (s.probe_ez) {
     const cudaError_t e = cudaMemcpyAsync(s.probe_ez + (t - 1), s.ez + (size_t)p.probe_i * p.ny + p.probe_j,
                                           sizeof(float), cudaMemcpyDeviceToDevice, st);
@@ -84,10 +81,6 @@ int step_per_function(int t, const fdtd2d_params& p, const fdtd2d_state& s, cuda
       return FDTD_ERR_CUDA;
     }
   }
-  if (p.nf > 0 && (rc = launch_fourier(t, p, s, st))) return rc;
-  if (tfsf && (rc = launch_hxinct(p, s, st))) return rc;
-  if ((rc = launch_hfield(p, s, st))) return rc;
-  if (tfsf && (rc = launch_incth(p, s, st))) return rc;
   return FDTD_OK;
 }
 
@@ -167,7 +160,7 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
 
   if (!fused_ok(p, s) || nsteps == 1) {
     for (int t = t0 + 1; t <= t0 + nsteps; ++t)
-      if ((rc = step_per_function(t, *p, *s, st))) return rc;
+      if ((rc = step_three_launches(t, *p, *s, st))) return rc;
     if (s->status) launch_check_finite(s->ez, (size_t)p->nx * p->ny, s->status, st);
     return fdtd_host::check_launch();
   }

@@ -19,6 +19,9 @@ int launch_inctdz(const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st
 int launch_hxinct(const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st);
 int launch_incth(const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st);
 int launch_fourier(int t, const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st);
+// one whole step (TF/SF, source, DFT included) in three launches, bitwise
+// equal to the per-function sequence
+int launch_step3(int t, const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st);
 int launch_dielectric(int nx, int ny, int npml, double rgrid, double dt, double epsr, double sigma, float* naz,
                       float* nbz, cudaStream_t st);
 int launch_check_finite(const float* x, size_t n, int* status, cudaStream_t st);

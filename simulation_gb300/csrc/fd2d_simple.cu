@@ -193,6 +193,134 @@ __global__ void k_check_finite(const float* __restrict__ x, size_t n, int* statu
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) raise_status(status, ST_NONFINITE);
 }
 
+// ================================================================ one step in three launches
+// The TF/SF + DFT program (fd2d/python/fd2d_3_4.py:268-277) runs nine
+// reference functions per step.  These three kernels do the same work in the
+// same per-cell order, so the result is bitwise equal to the nine per-function
+// launches:
+//   S1  ezinct (block 0, after its cells) | dfield + source + inctdz per cell;
+//   S2  efield + fourier per cell | hxinct + the input probe (block 0);
+//   S3  hfield + incthx + incthy per cell.
+// Race-free: S1 reads hxi and writes ezi/dz, S2 reads ezi and writes hxi/ez,
+// S3 reads ezi/ez and writes hx/hy; no kernel reads what a peer block writes.
+
+// S1: 2D grid of (32, 8) blocks; block (0, 0) also runs the incident line
+template <bool PML>
+__global__ void k_step_d(int nx, int ny, int npml, fdtd2d_pml pml, float* __restrict__ dz,
+                         const float* __restrict__ hx, const float* __restrict__ hy, int src_kind, int src_i,
+                         int src_j, const float* __restrict__ src_table, float* __restrict__ ezi,
+                         const float* __restrict__ hxi, float* __restrict__ bc, const float* __restrict__ tfsf_table,
+                         int t) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i < nx && j < ny) {
+    const size_t n = (size_t)i * ny + j;
+    const bool src_here = src_kind != FDTD_SRC_NONE && i == src_i && j == src_j;
+    const float src_val = src_here ? src_table[t - 1] : 0.f;
+    float d = dz[n];
+    if (i >= 1 && j >= 1) {
+      float gx3 = 1.f, gy3 = 1.f, gx2 = 1.f, gy2 = 1.f;
+      if (PML) {
+        gx3 = __ldg(pml.gx3 + i);
+        gy3 = __ldg(pml.gy3 + j);
+        gx2 = __ldg(pml.gx2 + i);
+        gy2 = __ldg(pml.gy2 + j);
+      }
+      d = d_update(d, hy[n], hy[n - ny], hx[n], hx[n - 1], gx3, gy3, gx2, gy2);
+    }
+    if (src_here) d = (src_kind == FDTD_SRC_HARD) ? src_val : __fadd_rn(d, src_val);
+    if (ezi && i >= npml - 1 && i <= nx - npml) {  // inctdz (fd2d/python/fd2d_3_4.py:123-127)
+      if (j == npml - 1) d = __fmaf_rn(0.5f, hxi[npml - 2], d);
+      if (j == ny - npml) d = __fmaf_rn(-0.5f, hxi[ny - npml], d);
+    }
+    dz[n] = d;
+  }
+  if (ezi && blockIdx.x == 0 && blockIdx.y == 0) {
+    // ezinct (fd2d/python/fd2d_3_4.py:103-110), then ezi[3] of dfield (:119)
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
+    for (int k = 1 + tid; k < ny; k += nth) ezi[k] = __fmaf_rn(0.5f, __fsub_rn(hxi[k - 1], hxi[k]), ezi[k]);
+    __syncthreads();
+    if (tid == 0) {
+      ezi[0] = bc[0];
+      bc[0] = bc[1];
+      bc[1] = ezi[1];
+      ezi[ny - 1] = bc[3];
+      bc[3] = bc[2];
+      bc[2] = ezi[ny - 2];
+      ezi[3] = tfsf_table[t - 1];
+    }
+  }
+}
+
+// S2: grid-stride over cells; block 0 also advances the incident hx line and
+// accumulates the input probe ezi[6]
+template <bool LOSSY>
+__global__ void k_step_e(size_t ncell, int ny, const float* __restrict__ naz, const float* __restrict__ nbz,
+                         const float* __restrict__ dz, float* __restrict__ iz, float* __restrict__ ez, int nf,
+                         const float* __restrict__ cs, const float* __restrict__ sn, float* __restrict__ r_pt,
+                         float* __restrict__ i_pt, const float* __restrict__ ezi, float* __restrict__ hxi,
+                         float* __restrict__ r_in, float* __restrict__ i_in) {
+  for (size_t n = blockIdx.x * (size_t)blockDim.x + threadIdx.x; n < ncell; n += (size_t)gridDim.x * blockDim.x) {
+    float e;
+    if (LOSSY) {
+      float izv = iz[n];
+      e = e_update_lossy(dz[n], izv, __ldg(naz + n), __ldg(nbz + n));
+      iz[n] = izv;
+    } else {
+      e = e_update(dz[n], __ldg(naz + n));
+    }
+    ez[n] = e;
+    for (int f = 0; f < nf; ++f) {  // fourier (fd2d/python/fd2d_3_4.py:90-99)
+      const size_t m = (size_t)f * ncell + n;
+      r_pt[m] = __fmaf_rn(cs[f], e, r_pt[m]);
+      i_pt[m] = __fmaf_rn(-sn[f], e, i_pt[m]);
+    }
+  }
+  if (blockIdx.x == 0 && ezi) {
+    if (threadIdx.x < nf) {
+      const int f = threadIdx.x;
+      r_in[f] = __fmaf_rn(cs[f], ezi[6], r_in[f]);
+      i_in[f] = __fmaf_rn(-sn[f], ezi[6], i_in[f]);
+    }
+    if (hxi)  // hxinct (fd2d/python/fd2d_3_4.py:140-143)
+      for (int k = threadIdx.x; k < ny - 1; k += blockDim.x) hxi[k] = __fmaf_rn(0.5f, __fsub_rn(ezi[k], ezi[k + 1]), hxi[k]);
+  }
+}
+
+// S3: hfield, then incthx/incthy on the TF/SF box edges (fd2d/python/fd2d_3_4.py:158-170)
+template <bool PML>
+__global__ void k_step_h(int nx, int ny, int npml, fdtd2d_pml pml, const float* __restrict__ ez,
+                         float* __restrict__ ihx, float* __restrict__ ihy, float* __restrict__ hx,
+                         float* __restrict__ hy, const float* __restrict__ ezi) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= nx - 1 || j >= ny - 1) return;
+  const size_t n = (size_t)i * ny + j;
+  const float e = ez[n];
+  float hxv = hx[n], hyv = hy[n];
+  if (PML) {
+    float ihxv = ihx[n], ihyv = ihy[n];
+    h_update_pml(e, ez[n + 1], ez[n + ny], hxv, hyv, ihxv, ihyv, __ldg(pml.fx1 + i), __ldg(pml.fx2 + i),
+                 __ldg(pml.fx3 + i), __ldg(pml.fy1 + j), __ldg(pml.fy2 + j), __ldg(pml.fy3 + j));
+    ihx[n] = ihxv;
+    ihy[n] = ihyv;
+  } else {
+    h_update_free(e, ez[n + 1], ez[n + ny], hxv, hyv);
+  }
+  if (ezi) {
+    if (i >= npml - 1 && i <= nx - npml) {
+      if (j == npml - 2) hxv = __fmaf_rn(0.5f, ezi[npml - 1], hxv);
+      if (j == ny - npml) hxv = __fmaf_rn(-0.5f, ezi[ny - npml], hxv);
+    }
+    if (j >= npml - 1 && j <= ny - npml) {
+      if (i == npml - 2) hyv = __fmaf_rn(-0.5f, ezi[j], hyv);
+      if (i == nx - npml) hyv = __fmaf_rn(0.5f, ezi[j], hyv);
+    }
+  }
+  hx[n] = hxv;
+  hy[n] = hyv;
+}
+
 // ================================================================ launchers
 static inline dim3 grid2d(int nx, int ny, dim3 blk) {
   return dim3((unsigned)((ny + blk.x - 1) / blk.x), (unsigned)((nx + blk.y - 1) / blk.y));
@@ -248,6 +376,46 @@ int launch_hxinct(const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st
 int launch_incth(const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st) {
   const int n = std::max(p.nx, p.ny) - 2 * p.tfsf_npml + 2;
   k_incth<<<(n + 255) / 256, 256, 0, st>>>(p.nx, p.ny, p.tfsf_npml, s.ezi, s.hx, s.hy);
+  return fdtd_host::check_launch();
+}
+
+int launch_step3(int t, const fdtd2d_params& p, const fdtd2d_state& s, cudaStream_t st) {
+  const dim3 blk(32, 8);
+  const bool tfsf = p.tfsf_npml > 0;
+  float* ezi = tfsf ? s.ezi : nullptr;
+  const int npml = p.tfsf_npml;
+  if (has_pml(p))
+    k_step_d<true><<<grid2d(p.nx, p.ny, blk), blk, 0, st>>>(p.nx, p.ny, npml, p.pml, s.dz, s.hx, s.hy, p.src.kind,
+                                                            p.src.i, p.src.j, p.src.table, ezi, s.hxi, s.bc,
+                                                            p.tfsf_table, t);
+  else
+    k_step_d<false><<<grid2d(p.nx, p.ny, blk), blk, 0, st>>>(p.nx, p.ny, npml, p.pml, s.dz, s.hx, s.hy, p.src.kind,
+                                                             p.src.i, p.src.j, p.src.table, ezi, s.hxi, s.bc,
+                                                             p.tfsf_table, t);
+  int rc = fdtd_host::check_launch();
+  if (rc) return rc;
+  const size_t ncell = (size_t)p.nx * p.ny;
+  const int blocks = (int)std::min<size_t>((ncell + 255) / 256, (size_t)152 * 16);
+  const int nf = p.nf > 0 ? p.nf : 0;
+  const float* cs = nf ? p.dft_cos + (size_t)(t - 1) * nf : nullptr;
+  const float* sn = nf ? p.dft_sin + (size_t)(t - 1) * nf : nullptr;
+  // the input probe ezi[6] is accumulated only when the DFT is on (as fourier does)
+  const float* ezi_e = tfsf ? s.ezi : nullptr;
+  float* r_in = nf ? s.r_in : nullptr;
+  float* i_in = nf ? s.i_in : nullptr;
+  if (p.nbz)
+    k_step_e<true><<<blocks, 256, 0, st>>>(ncell, p.ny, p.naz, p.nbz, s.dz, s.iz, s.ez, nf, cs, sn, s.r_pt, s.i_pt,
+                                           ezi_e, tfsf ? s.hxi : nullptr, r_in, i_in);
+  else
+    k_step_e<false><<<blocks, 256, 0, st>>>(ncell, p.ny, p.naz, nullptr, s.dz, nullptr, s.ez, nf, cs, sn, s.r_pt,
+                                            s.i_pt, ezi_e, tfsf ? s.hxi : nullptr, r_in, i_in);
+  if ((rc = fdtd_host::check_launch())) return rc;
+  if (has_pml(p))
+    k_step_h<true><<<grid2d(p.nx, p.ny, blk), blk, 0, st>>>(p.nx, p.ny, npml, p.pml, s.ez, s.ihx, s.ihy, s.hx, s.hy,
+                                                            ezi);
+  else
+    k_step_h<false><<<grid2d(p.nx, p.ny, blk), blk, 0, st>>>(p.nx, p.ny, npml, p.pml, s.ez, nullptr, nullptr, s.hx,
+                                                             s.hy, ezi);
   return fdtd_host::check_launch();
 }
 

@@ -158,33 +158,45 @@ __global__ void k_propagation(int n, int nbins, const float* __restrict__ feat, 
   }
   double Kr[2] = {0.0, 0.0}, Ki[2] = {0.0, 0.0};
   float2 kc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-  float ce = -1.f, cs = -1.f;
-  int run = 0;
-  for (int c = probe_in; c < probe_out; ++c) {
-    float e, s;
-    cell_material(f, nbins, c, e, s);
-    if (e != ce || s != cs) {  // warp-uniform: every lane reads the same cell
+  float ce = -1.f, cs = -1.f;  // current material (none yet: the first cell starts a run)
+  int run_start = probe_in;
+  // 32 cells per iteration, one per lane; material changes found by ballot and
+  // handled in order by the whole warp (each lane for its two frequencies)
+  for (int c0 = probe_in; c0 < probe_out; c0 += 32) {
+    const int c = c0 + lane;
+    float e = 0.f, s = 0.f;
+    if (c < probe_out) cell_material(f, nbins, c, e, s);
+    float pe = __shfl_up_sync(0xffffffffu, e, 1), ps = __shfl_up_sync(0xffffffffu, s, 1);
+    if (lane == 0) {
+      pe = ce;
+      ps = cs;
+    }
+    unsigned chg = __ballot_sync(0xffffffffu, c < probe_out && (e != pe || s != ps));
+    while (chg) {
+      const int pos = __ffs(chg) - 1;
+      chg &= chg - 1;
+      const int run = c0 + pos - run_start;
       for (int q = 0; q < 2; ++q) {
         Kr[q] = fma((double)run, (double)kc[q].x, Kr[q]);
         Ki[q] = fma((double)run, (double)kc[q].y, Ki[q]);
       }
-      run = 0;
-      ce = e;
-      cs = s;
-      if (e == 0.f && s == 0.f) {
+      run_start = c0 + pos;
+      ce = __shfl_sync(0xffffffffu, e, pos);
+      cs = __shfl_sync(0xffffffffu, s, pos);
+      if (ce == 0.f && cs == 0.f) {
         kc[0] = k0[0];
         kc[1] = k0[1];
       } else {
         // the FDTD's float32 coefficients (lossy layer formula of fd1d/program/fd1d_1_5.py:37-44)
-        const double er = 1.0 + eps_scale * (double)e, sg = sig_scale * (double)s;
+        const double er = 1.0 + eps_scale * (double)ce, sg = sig_scale * (double)cs;
         const double eaf = loss_scale * sg / er;
         const float ca = (float)((1.0 - eaf) / (1.0 + eaf));
         const float inv_cb = 1.0f / (float)(0.5 / (er * (1.0 + eaf)));
         for (int q = 0; q < 2; ++q) kc[q] = on[q] ? yee_wavenumber(ca, inv_cb, sh[q], ch[q]) : make_float2(0.f, 0.f);
       }
     }
-    ++run;
   }
+  const int run = probe_out - run_start;
   for (int q = 0; q < 2; ++q) {
     Kr[q] = fma((double)run, (double)kc[q].x, Kr[q]);
     Ki[q] = fma((double)run, (double)kc[q].y, Ki[q]);

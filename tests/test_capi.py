@@ -76,3 +76,29 @@ def test_argument_checks_without_gpu(lib):
     q.form = 0
     assert lib.fdtd1d_step_n(C.byref(q), C.byref(t), 0, 1, None) == -1  # cb missing
     assert lib.fdtd2d_dielectric_cylinder(64, 64, 40, 10.0, 1e-11, 30.0, 0.3, fake, fake, None) == -2
+
+
+def test_surrogate_and_gemm_argument_checks_without_gpu(lib):
+    """The surrogate helpers and the tensor-core GEMM validate on the host too."""
+    from simulation_gb300 import _lib
+    fake = C.c_void_p(0x10000)
+    d = C.c_double
+    # propagation frame: NULL pointers, then bad sizes (nf > 64, n < 1, negative probes)
+    assert lib.fno_propagation(4, 2048, None, 64, fake, d(8.0), d(0.05), d(1.0), 30, 10, fake, None) == -1
+    assert lib.fno_propagation(4, 2048, fake, 65, fake, d(8.0), d(0.05), d(1.0), 30, 10, fake, None) == -2
+    assert lib.fno_propagation(0, 2048, fake, 64, fake, d(8.0), d(0.05), d(1.0), 30, 10, fake, None) == -2
+    assert lib.fno_propagation(4, 2048, fake, 64, fake, d(8.0), d(0.05), d(1.0), -1, 10, fake, None) == -2
+    assert lib.fno_propagation(4, 2048, fake, 64, fake, d(0.0), d(0.05), d(1.0), 30, 10, fake, None) == -2
+    assert lib.fno_cmul(4, 64, None, fake, 0, fake, None) == -1
+    assert lib.fno_cmul(0, 64, fake, fake, 0, fake, None) == -2
+    # lift: at most 8 input channels
+    assert lib.fno_lift_fwd(16, 128, 9, fake, fake, fake, fake, None) == -2
+    assert lib.fno_lift_bwd(16, 128, 0, fake, fake, fake, fake, None) == -2
+    assert lib.fno_rel_mse(4, 128, C.c_float(0.0), fake, fake, fake, fake, None) == -2
+    # GEMM descriptor: NULL, then a non-16-byte-aligned leading dimension
+    assert lib.fdtd_gemm_bf16(None, None, None) == -1
+    g = _lib.GemmDesc()
+    g.M, g.N, g.K, g.batch = 128, 128, 64, 1
+    g.A, g.B, g.C32 = 0x10000, 0x10000, 0x10000
+    g.lda, g.ldb, g.ldc = 65, 64, 128  # 65 BF16 = 130 bytes per row
+    assert lib.fdtd_gemm_bf16(C.byref(g), None, None) < 0

@@ -39,6 +39,30 @@ def _program_sim(name):
     raise KeyError(name)
 
 
+@pytest.mark.parametrize("nx,ny", [(100, 100), (97, 83)])
+def test_three_launch_step_bitwise_equals_nine_functions(cuda_lib, nx, ny):
+    """With TF/SF, the DFT and a lossy map on, fdtd2d_step_n runs each step as
+    three launches; every field, the incident line, its ABC state and the DFT
+    accumulators equal the nine per-function launches bit for bit."""
+    from simulation_gb300 import fd2d as G
+    dt = 0.01 / 6e8
+
+    def make():
+        naz, nbz = G.dielectric(nx, ny, 8, 14, dt, 30.0, 0.30)
+        return G.SimTM2D(nx, ny, pml=G.pmlparam(nx, ny, 8), naz=naz, nbz=nbz, lossy=True, tfsf_npml=8,
+                         freq=[50e6, 300e6, 700e6], dt=dt,
+                         source=G.PointSource(nx // 3, ny // 3, ("sin", 0.01, 900e6), "soft"))
+    a, b = make(), make()
+    a.step(150)
+    b.step_per_function(150)
+    torch.cuda.synchronize()
+    for k in a.FIELDS:
+        x, y = getattr(a, k), getattr(b, k)
+        if x is None:
+            continue
+        assert torch.equal(x, y), f"{k} differs"
+
+
 @pytest.mark.parametrize("name", ["fd2d_3_1", "fd2d_3_2", "fd2d_3_3", "fd2d_3_4"])
 @pytest.mark.parametrize("path", ["fused", "per_function"])
 def test_program_vs_golden(cuda_lib, golden, name, path):
