@@ -156,7 +156,9 @@ size_t fdtd2d_workspace_size(const fdtd2d_params* p, int steps_per_pass);
  * pass over HBM; `workspace` (fdtd2d_workspace_size bytes, 256-byte aligned)
  * holds the ping-pong copy of the evolving fields.  Results land in the
  * caller's arrays, bitwise equal to calling dfield/efield/hfield per step.
- * With TF/SF or DFT enabled the per-function kernels run instead.
+ * With TF/SF or DFT enabled each step runs as three launches (D + ezinct +
+ * inctdz; E + fourier + hxinct; H + incthx + incthy), bitwise equal to the nine
+ * per-function calls.
  * Replaces the `for t in 1..ns` loops of fd2d/python/fd2d_3_2.py:139-142 and
  * fd2d/cuda/fd2d_3_4.cu:327-336. */
 int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass,
