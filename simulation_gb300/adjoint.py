@@ -10,8 +10,9 @@ Forward: the fused kernel (``fdtd2d_step_n``) runs the time loop, records
 Ez at the probe every step and copies the fields to a checkpoint every
 ``checkpoint`` steps.  Reverse: for each segment, last first, the states of
 the segment are recomputed from its checkpoint (``fdtd2d_pass``, one step per
-pass, bitwise equal to the forward), then ``fdtd2d_adjoint_step`` walks the
-segment backwards accumulating dJ/dnaz on the design box;
+pass, bitwise equal to the forward; on a second stream, one segment ahead of
+the sweep), then ``fdtd2d_adjoint_step`` walks the segment backwards
+accumulating dJ/dnaz on the design box;
 dJ/deps_r = -naz^2 * dJ/dnaz since naz = 1/(eps_r + sigma*dt/eps0).
 
 ``FdtdObjective`` wraps forward + reverse as a torch.autograd.Function.
@@ -63,7 +64,7 @@ class AdjointProblem:
         self.ncp = -(-ns // checkpoint)
         z = lambda *s: torch.zeros(s, dtype=torch.float32, device=self.device)  # noqa: E731
         self.ckpt = z(self.ncp, 6, nx, ny)
-        self.seg = z(checkpoint, 6, nx, ny)
+        self.seg = z(2, checkpoint, 6, nx, ny)  # two segments: one recomputed while the other is swept
         self.adj = z(6, nx, ny)
         self.tmp = z(nx, ny)
         self.ez_scratch = z(nx, ny)
@@ -104,34 +105,61 @@ class AdjointProblem:
 
     # ------------------------------------------------------------ reverse
     def gradient_naz(self) -> torch.Tensor:
-        """dJ/dnaz on the design box (float32 [bi][bj]) by the reverse sweep."""
+        """dJ/dnaz on the design box (float32 [bi][bj]) by the reverse sweep.
+
+        Segments are swept last first.  While the current stream walks segment
+        c backwards, a second stream recomputes the states of segment c-1 into
+        the other half of ``seg``; events order each buffer's reuse.  The work
+        per kernel is unchanged, so the gradient is the same bit for bit."""
         lib = _lib.lib()
-        st = _lib.stream_ptr()
+        main = torch.cuda.current_stream(self.device)
+        if not hasattr(self, "_side"):
+            self._side = torch.cuda.Stream(device=self.device)
+        side = self._side
+        st_main, st_side = main.cuda_stream, side.cuda_stream
         p = self.sim._p
         self.adj.zero_()
         self.grad_naz.zero_()
         adj = self._fields(self.adj)
         i0, j0, bi, bj = self.box
         box = _lib.Box2D(i0, j0, bi, bj)
-        seg_f = [self._fields(self.seg[k]) for k in range(self.cp)]
-        for c in reversed(range(self.ncp)):
+        seg_f = [[self._fields(self.seg[b, k]) for k in range(self.cp)] for b in range(2)]
+        ready = [torch.cuda.Event(), torch.cuda.Event()]  # buffer b holds its segment's states
+        free = [torch.cuda.Event(), torch.cuda.Event()]   # the sweep over buffer b has finished
+        side.wait_stream(main)  # the forward's checkpoints and the zeroing above come first
+
+        def recompute(c: int, b: int) -> list:
             t_start = c * self.cp
             L = min(self.cp, self.ns - t_start)
-            ck = self._fields(self.ckpt[c])
-            states = [ck]
+            states = [self._fields(self.ckpt[c])] + seg_f[b][1:L]
             for k in range(1, L):
-                out = seg_f[k]
-                rc = lib.fdtd2d_pass(C.byref(p), C.byref(states[-1]), C.byref(out), self.ez_scratch.data_ptr(),
-                                     t_start + k - 1, 1, None, st)
+                rc = lib.fdtd2d_pass(C.byref(p), C.byref(states[k - 1]), C.byref(states[k]),
+                                     self.ez_scratch.data_ptr(), t_start + k - 1, 1, None, st_side)
                 if rc:
                     raise _lib.FdtdError(rc, "fdtd2d_pass")
-                states.append(out)
+            ready[b].record(side)
+            return states
+
+        order = list(reversed(range(self.ncp)))
+        states_of = {order[0]: recompute(order[0], 0)}
+        for idx, c in enumerate(order):
+            b = idx % 2
+            if idx + 1 < len(order):
+                nb = 1 - b
+                if idx >= 1:
+                    side.wait_event(free[nb])  # the sweep of the segment before used buffer nb
+                states_of[order[idx + 1]] = recompute(order[idx + 1], nb)
+            main.wait_event(ready[b])
+            states = states_of.pop(c)
+            t_start = c * self.cp
+            L = min(self.cp, self.ns - t_start)
             for t in range(t_start + L, t_start, -1):
                 rc = lib.fdtd2d_adjoint_step(t, C.byref(p), C.byref(states[t - t_start - 1]), C.byref(adj),
                                              self.tmp.data_ptr(), self.probe[0], self.probe[1], 2.0, box,
-                                             self.grad_naz.data_ptr(), None, st)
+                                             self.grad_naz.data_ptr(), None, st_main)
                 if rc:
                     raise _lib.FdtdError(rc, "fdtd2d_adjoint_step")
+            free[b].record(main)
         return self.grad_naz
 
     def gradient_eps(self) -> torch.Tensor:
