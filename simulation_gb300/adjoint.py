@@ -41,7 +41,8 @@ class AdjointProblem:
 
     def __init__(self, nx: int = 1024, ny: int = 1024, npml: int = 16, box=(256, 256), src_offset: int = 200,
                  probe_offset: int = 200, ns: int = 3000, checkpoint: int = 64, wave=("gauss", 40, 12.0),
-                 src_kind: str = "soft", sigma_box: float = 0.0, grade: float = 0.33, device="cuda"):
+                 src_kind: str = "soft", sigma_box: float = 0.0, grade: float = 0.33, device="cuda",
+                 use_graphs: bool = True):
         if ny % 4:
             raise ValueError("ny must be a multiple of 4")
         self.nx, self.ny, self.ns, self.cp = nx, ny, ns, checkpoint
@@ -70,6 +71,11 @@ class AdjointProblem:
         self.ez_scratch = z(nx, ny)
         self.grad_naz = z(bi, bj)
         self.J = None
+        # the loops are static for a problem (pointers, steps, segment order):
+        # from the second call on, each sweep replays a CUDA graph of itself
+        self.use_graphs = use_graphs
+        self._graph = {"forward": None, "reverse": None}
+        self._warm = {"forward": False, "reverse": False}
 
     # ------------------------------------------------------------ material
     def set_eps(self, eps_box: torch.Tensor) -> None:
@@ -91,15 +97,39 @@ class AdjointProblem:
         return f
 
     # ------------------------------------------------------------ forward
+    def _run(self, name: str, body) -> None:
+        """body() eagerly on the first call; later calls capture it once into a
+        CUDA graph and replay that (same kernels, same arguments)."""
+        if not self.use_graphs or not self._warm[name]:
+            body()
+            self._warm[name] = True
+            return
+        g = self._graph[name]
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            cap = torch.cuda.Stream(device=self.device)
+            cap.wait_stream(torch.cuda.current_stream(self.device))
+            with torch.cuda.stream(cap):
+                with torch.cuda.graph(g, stream=cap):
+                    body()
+            torch.cuda.current_stream(self.device).wait_stream(cap)
+            self._graph[name] = g
+        g.replay()
+
     def forward(self) -> float:
         """Run the time loop with checkpoints; returns J = sum_t Ez_t(probe)^2."""
         s = self.sim
-        s.reset()
-        self.trace.zero_()
-        for c in range(self.ncp):
-            for k, name in enumerate(self.FIELDS):
-                self.ckpt[c, k].copy_(getattr(s, name))
-            s.step(min(self.cp, self.ns - c * self.cp))
+
+        def body():
+            s.reset()
+            self.trace.zero_()
+            for c in range(self.ncp):
+                for k, name in enumerate(self.FIELDS):
+                    self.ckpt[c, k].copy_(getattr(s, name))
+                s.step(min(self.cp, self.ns - c * self.cp))
+
+        self._run("forward", body)
+        s.t = self.ns
         self.J = float((self.trace.double() ** 2).sum())
         return self.J
 
@@ -111,10 +141,14 @@ class AdjointProblem:
         c backwards, a second stream recomputes the states of segment c-1 into
         the other half of ``seg``; events order each buffer's reuse.  The work
         per kernel is unchanged, so the gradient is the same bit for bit."""
-        lib = _lib.lib()
-        main = torch.cuda.current_stream(self.device)
         if not hasattr(self, "_side"):
             self._side = torch.cuda.Stream(device=self.device)
+        self._run("reverse", self._reverse)
+        return self.grad_naz
+
+    def _reverse(self) -> None:
+        lib = _lib.lib()
+        main = torch.cuda.current_stream(self.device)
         side = self._side
         st_main, st_side = main.cuda_stream, side.cuda_stream
         p = self.sim._p
@@ -160,7 +194,6 @@ class AdjointProblem:
                 if rc:
                     raise _lib.FdtdError(rc, "fdtd2d_adjoint_step")
             free[b].record(main)
-        return self.grad_naz
 
     def gradient_eps(self) -> torch.Tensor:
         """dJ/deps_r on the design box (float64): -naz^2 * dJ/dnaz."""

@@ -43,6 +43,30 @@ def test_checkpoint_interval_does_not_change_gradient(cuda_lib):
     assert torch.equal(a.gradient_naz(), b.gradient_naz())
 
 
+def test_graph_replay_equals_eager(cuda_lib):
+    """From the second call on, forward and reverse replay captured CUDA
+    graphs: J and the gradient equal the eager sweeps bit for bit, also after
+    the permittivity changes (the graphs read naz/nbz in place)."""
+    a, eps = _small(cp=16)
+    b, _ = _small(cp=16)
+    b.use_graphs = False
+    a.set_eps(eps)
+    b.set_eps(eps)
+    for _ in range(3):  # eager, capture + replay, replay
+        ja = a.forward()
+        ga = a.gradient_naz().clone()
+    assert a._graph["forward"] is not None and a._graph["reverse"] is not None
+    jb = b.forward()
+    gb = b.gradient_naz().clone()
+    assert ja == jb
+    assert torch.equal(ga, gb)
+    eps2 = eps * 1.1
+    a.set_eps(eps2)
+    b.set_eps(eps2)
+    assert a.forward() == b.forward()
+    assert torch.equal(a.gradient_naz(), b.gradient_naz())
+
+
 def test_adjoint_vs_central_fd_config4(cuda_lib):
     """1024^2, 16-cell PML, 256^2 design box, 3000 steps, checkpoints every 64:
     the reverse kernel's dJ/deps on 32 random cells vs central differences with
