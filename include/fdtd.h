@@ -384,7 +384,8 @@ typedef struct {
 
 typedef struct {
   float* spec;      /* device [nruns][4][nf]: re/im at the entry probe, re/im at the exit probe */
-  int* done;        /* device [nruns] or NULL: 1 when the run completed */
+  int* done;        /* device [nruns] or NULL: set to 1 when a run of the plan completes;
+                       not cleared by the call (zero it once before the groups' calls) */
   int* status;      /* device status word or NULL */
   unsigned* queue;  /* device work counter (one unsigned), reset by the call */
 } fdtd1d_batch_out;

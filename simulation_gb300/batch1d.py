@@ -209,6 +209,7 @@ class BatchRunner:
         nsteps = self.nsteps if nsteps is None else nsteps
         p = self._params(nsteps)
         st = _lib.stream_ptr()
+        self.done.zero_()  # each group's launch sets the flags of its own runs
         for g, grp in enumerate(self.tuning["groups"]):
             runs = np.nonzero((self.batch.ke > grp["ke_lo"]) & (self.batch.ke <= grp["ke_hi"]))[0]
             if runs.size == 0:

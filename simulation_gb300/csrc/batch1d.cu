@@ -348,13 +348,9 @@ int fdtd1d_batch_run(const fdtd1d_batch_params* p, fdtd1d_batch_out* o, const in
     fdtd_host::note_cuda_error(e);
     return FDTD_ERR_CUDA;
   }
-  if (o->done) {
-    e = cudaMemsetAsync(o->done, 0, sizeof(int) * (size_t)p->nruns, st);
-    if (e != cudaSuccess) {
-      fdtd_host::note_cuda_error(e);
-      return FDTD_ERR_CUDA;
-    }
-  }
+  // done[] is not cleared here: a plan may cover only some of the runs (one
+  // call per tuning group), and clearing all nruns flags would erase the
+  // flags an earlier group's launch set.  The caller zeroes done[] once.
   fdtd::BatchArgs A{};
   A.p = *p;
   A.o = *o;

@@ -5,6 +5,8 @@
 // partial sums, MSE loss and Adam.  No reference counterpart.
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "fdtd_common.cuh"
 
 namespace fdtd {
@@ -50,6 +52,43 @@ __global__ void k_lift_fwd(size_t rows, int C, int cin, const float* __restrict_
 }
 
 constexpr int kLiftMaxIn = 8;
+
+// The same lift, one thread per (row, 8 channels), 32-bit indices: block
+// (C/8, 256/(C/8)) threads, x = channel group, y = row; the row's inputs are
+// read once per thread and the 8 BF16 results leave as one 16-byte store.
+// Same accumulation order per element as k_lift_fwd, so results are identical.
+__global__ void k_lift_fwd8(int rows, int C, int cin, const float* __restrict__ in, const float* __restrict__ P,
+                            const float* __restrict__ p, bf16* __restrict__ x0) {
+  const int c0 = threadIdx.x * 8;
+  // this thread's 8 x cin weights and 8 biases stay in registers for all its rows
+  float pv[8], pw[8][kLiftMaxIn];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    pv[k] = p[c0 + k];
+#pragma unroll
+    for (int j = 0; j < kLiftMaxIn; ++j) pw[k][j] = j < cin ? P[(c0 + k) * cin + j] : 0.f;
+  }
+  for (int r = blockIdx.x * blockDim.y + threadIdx.y; r < rows; r += gridDim.x * blockDim.y) {
+    float v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = pv[k];
+#pragma unroll
+    for (int j = 0; j < kLiftMaxIn; ++j) {
+      if (j < cin) {
+        const float xj = in[(size_t)r * cin + j];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = fmaf(pw[k][j], xj, v[k]);
+      }
+    }
+    uint32_t w[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+      w[k] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    *reinterpret_cast<uint4*>(x0 + (size_t)r * C + c0) = make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
 
 // dP[c][j] += sum_r dx0[r][c]*in[r][j]; dp[c] += sum_r dx0[r][c]   (block per channel group)
 __global__ void k_lift_bwd(size_t rows, int C, int cin, const float* __restrict__ in, const bf16* __restrict__ dx0,
@@ -225,8 +264,48 @@ __global__ void k_cmul(size_t n, int nf, const float* __restrict__ P, const floa
   }
 }
 
-// DFT layout [B][C][2M] (cos rows 0..M-1, -sin rows M..2M-1) -> mode-major
-// [M][B][2C] with [Re | Im] along the last axis; and the inverse permute
+// DFT layout [B][C][2M] (cos rows 0..M-1, -sin rows M..2M-1) <-> mode-major
+// [M][B][2C] with [Re | Im] along the last axis.  One block per sample b,
+// through shared memory, so that both the [C][2M] side (rows of 2M) and the
+// mode-major side (rows of C for each (k, part)) are read and written in
+// contiguous runs.  The scalar versions are kept for shapes that do not fit.
+constexpr int kPermSmem = 128 * 64 + 256;  // staged floats per block: 2M rows of C+1 (padded), 33 KB
+
+__global__ void k_dft_to_modes_t(int B, int C, int M, const float* __restrict__ F, bf16* __restrict__ Fm) {
+  __shared__ float t[kPermSmem];
+  const int b = blockIdx.x;
+  const int W = 2 * M, n = C * W;
+  const float* src = F + (size_t)b * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int c = i / W, j = i - c * W;
+    t[j * (C + 1) + c] = src[i];  // padded row: transposed reads below are conflict-free
+  }
+  __syncthreads();
+  // destination rows: (k, part) -> Fm[k][b][part*C + c], c contiguous
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int j = i / C, c = i - j * C;  // j = part*M + k
+    const int part = j / M, k = j - part * M;
+    Fm[((size_t)k * B + b) * 2 * C + part * C + c] = __float2bfloat16_rn(t[j * (C + 1) + c]);
+  }
+}
+
+__global__ void k_modes_to_dft_t(int B, int C, int M, const float* __restrict__ Gm, bf16* __restrict__ G) {
+  __shared__ float t[kPermSmem];
+  const int b = blockIdx.x;
+  const int W = 2 * M, n = C * W;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int j = i / C, c = i - j * C;  // j = part*M + k
+    const int part = j / M, k = j - part * M;
+    t[j * (C + 1) + c] = Gm[((size_t)k * B + b) * 2 * C + part * C + c];
+  }
+  __syncthreads();
+  bf16* dst = G + (size_t)b * n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int c = i / W, j = i - c * W;
+    dst[i] = __float2bfloat16_rn(t[j * (C + 1) + c]);
+  }
+}
+
 __global__ void k_dft_to_modes(int B, int C, int M, const float* __restrict__ F, bf16* __restrict__ Fm) {
   const size_t total = (size_t)B * C * 2 * M;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
@@ -302,6 +381,39 @@ __global__ void k_meanpool(int B, int N, int C, const bf16* __restrict__ x, bf16
     float s = 0.f;
     for (int n = 0; n < N; ++n) s += __bfloat162float(x[((size_t)b * N + n) * C + c]);
     h[(size_t)b * C + c] = __float2bfloat16_rn(s / N);
+  }
+}
+
+// The same mean with 16-byte loads: thread (g, y) of a 256-thread block sums
+// channels 8g..8g+7 over rows y, y + ry, ...; the ry partial sums are added
+// in shared memory in a fixed order (C % 8 == 0, C / 8 <= 256).
+__global__ void k_meanpool8(int B, int N, int C, const bf16* __restrict__ x, bf16* __restrict__ h) {
+  __shared__ float part[256 * 8];
+  const int b = blockIdx.x;
+  const int groups = C / 8, ry = blockDim.x / groups;
+  const int g = threadIdx.x % groups, y = threadIdx.x / groups;
+  float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (y < ry) {
+    const bf16* base = x + (size_t)b * N * C + g * 8;
+    for (int n = y; n < N; n += ry) {
+      const uint4 u = *reinterpret_cast<const uint4*>(base + (size_t)n * C);
+      const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const __nv_bfloat162 h2 = *reinterpret_cast<const __nv_bfloat162*>(&w[e]);
+        s[2 * e] += __low2float(h2);
+        s[2 * e + 1] += __high2float(h2);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) part[(y * groups + g) * 8 + k] = s[k];
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    const int gg = c / 8, k = c % 8;
+    float t = 0.f;
+    for (int yy = 0; yy < ry; ++yy) t += part[(yy * groups + gg) * 8 + k];
+    h[(size_t)b * C + c] = __float2bfloat16_rn(t / N);
   }
 }
 
@@ -434,6 +546,11 @@ int fno_lift_fwd(long long rows, int C, int cin, const float* in, const float* P
                  fdtd_stream_t stream) {
   if (!in || !P || !p || !x0) return FDTD_ERR_NULL;
   if (rows < 1 || C < 1 || cin < 1 || cin > fdtd::kLiftMaxIn) return FDTD_ERR_SIZE;
+  if (C % 8 == 0 && C <= 2048 && rows < (1LL << 31) && ((uintptr_t)x0 & 15) == 0) {
+    const dim3 blk(C / 8, std::max(1, 256 / (C / 8)));
+    const long long nblk = std::min<long long>((rows + blk.y - 1) / blk.y, 152LL * 16);
+    FNO_LAUNCH(fdtd::k_lift_fwd8, dim3((unsigned)nblk), blk, (int)rows, C, cin, in, P, p, (bf16*)x0);
+  }
   FNO_LAUNCH(fdtd::k_lift_fwd, fdtd::grid1((size_t)rows * C), 256, (size_t)rows, C, cin, in, P, p, (bf16*)x0);
 }
 
@@ -464,12 +581,16 @@ int fno_cmul(long long n, int nf, const float* P, const float* y, int conj_p, fl
 int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_t stream) {
   if (!F || !Fm) return FDTD_ERR_NULL;
   if (B < 1 || C < 1 || M < 1) return FDTD_ERR_SIZE;
+  if ((C + 1) * 2 * M <= fdtd::kPermSmem)
+    FNO_LAUNCH(fdtd::k_dft_to_modes_t, dim3(B), 256, B, C, M, F, (bf16*)Fm);
   FNO_LAUNCH(fdtd::k_dft_to_modes, fdtd::grid1((size_t)B * C * 2 * M), 256, B, C, M, F, (bf16*)Fm);
 }
 
 int fno_modes_to_dft(int B, int C, int M, const float* Gm, void* G, fdtd_stream_t stream) {
   if (!Gm || !G) return FDTD_ERR_NULL;
   if (B < 1 || C < 1 || M < 1) return FDTD_ERR_SIZE;
+  if ((C + 1) * 2 * M <= fdtd::kPermSmem)
+    FNO_LAUNCH(fdtd::k_modes_to_dft_t, dim3(B), 256, B, C, M, Gm, (bf16*)G);
   FNO_LAUNCH(fdtd::k_modes_to_dft, fdtd::grid1((size_t)B * C * 2 * M), 256, B, C, M, Gm, (bf16*)G);
 }
 
@@ -501,6 +622,8 @@ int fno_gelu_fwd(long long n, const float* z, void* y, void* pre, fdtd_stream_t 
 int fno_meanpool(int B, int N, int C, const void* x, void* h, fdtd_stream_t stream) {
   if (!x || !h) return FDTD_ERR_NULL;
   if (B < 1 || N < 1 || C < 1) return FDTD_ERR_SIZE;
+  if (C % 8 == 0 && C / 8 <= 256 && ((uintptr_t)x & 15) == 0)
+    FNO_LAUNCH(fdtd::k_meanpool8, dim3(B), 256, B, N, C, (const bf16*)x, (bf16*)h);
   FNO_LAUNCH(fdtd::k_meanpool, dim3(B), 128, B, N, C, (const bf16*)x, (bf16*)h);
 }
 

@@ -102,10 +102,17 @@ def profile_features(batch: "B1.SlabBatch", idx=None, nbins: int = NBINS) -> np.
     return out
 
 
+_WDT = {}
+
+
 def propagation(inp: torch.Tensor, freqs=FREQS, dt: float | None = None) -> torch.Tensor:
     """[B][2*nf] float32 frame P of each profile (``fno_propagation``)."""
     dt = B1.DT if dt is None else dt
-    wdt = torch.as_tensor(2 * np.pi * np.asarray(freqs, dtype=np.float64) * dt, device=inp.device)
+    key = (str(inp.device), float(dt), tuple(np.asarray(freqs, dtype=np.float64).tolist()))
+    wdt = _WDT.get(key)
+    if wdt is None:  # device copy made once (a copy per call would also break CUDA-graph capture)
+        wdt = torch.as_tensor(2 * np.pi * np.asarray(freqs, dtype=np.float64) * dt, device=inp.device)
+        _WDT[key] = wdt
     nf = wdt.numel()
     P = torch.empty((inp.shape[0], 2 * nf), dtype=torch.float32, device=inp.device)
     _call("fno_propagation", inp.shape[0], inp.shape[1], inp.data_ptr(), nf, wdt.data_ptr(), EPS_SCALE, SIG_SCALE,

@@ -40,13 +40,17 @@ def test_sampled_runs_vs_oracle(cuda_lib):
 
 def test_tuning_does_not_change_results(cuda_lib):
     from simulation_gb300 import batch1d as B
-    batch = B.slab_batch(300, seed=11, ke_range=(500, 6000))
+    batch = B.slab_batch(300, seed=11, ke_range=(500, 20000))  # long enough for two-group splits
     outs = []
-    for tun in B.candidate_tunings(batch.ke)[:6]:
+    tunings = B.candidate_tunings(batch.ke)
+    assert any(len(t["groups"]) > 1 for t in tunings)
+    for tun in tunings:
         r = B.BatchRunner(batch, nsteps=600, tuning=tun)
         r.run()
         torch.cuda.synchronize()
         outs.append(r.spec.clone())
+        # every run of every group is flagged done, whatever the split
+        assert int(r.done.sum()) == batch.nruns, tun
     for o in outs[1:]:
         assert torch.equal(o, outs[0])
 
