@@ -150,6 +150,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint64_t* tfull = bars + 2 * STAGES;
   uint64_t* tempty = bars + 2 * STAGES + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 4);
+  // the bias of a one-column-tile GEMM (N <= BN: the same BN columns for every
+  // tile) is staged once, so the epilogue reads it from shared memory
+  float* sbias = reinterpret_cast<float*>(bars + 2 * STAGES + 6);  // 16-byte aligned for float4 reads
 
   const int warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
@@ -158,6 +161,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int mt = (a.M + BM - 1) / BM;
   const int nt = (a.N + BN - 1) / BN;
   const long long total = (long long)mt * nt * a.batch;
+  const bool bias_smem = a.bias != nullptr && nt == 1;
+  if (bias_smem)
+    for (int c = threadIdx.x; c < BN; c += blockDim.x) sbias[c] = c < a.N ? a.bias[c] : 0.f;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -311,9 +317,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   #pragma unroll
         for (int q = 0; q < 32; ++q) z[q] = __fmul_rn(a.alpha, __uint_as_float(r[q]));
         if (a.bias) {
+          const float* bsrc = bias_smem ? sbias + c0 : a.bias + col0;
   #pragma unroll
           for (int v = 0; v < 8; ++v) {
-            const float4 b = *reinterpret_cast<const float4*>(a.bias + col0 + 4 * v);
+            const float4 b = *reinterpret_cast<const float4*>(bsrc + 4 * v);
             z[4 * v] = __fadd_rn(z[4 * v], b.x);
             z[4 * v + 1] = __fadd_rn(z[4 * v + 1], b.y);
             z[4 * v + 2] = __fadd_rn(z[4 * v + 2], b.z);
@@ -435,7 +442,7 @@ int make_map(CUtensorMap* tm, const void* base, uint64_t inner, uint64_t outer, 
 
 template <int BN, int STAGES>
 size_t smem_bytes() {
-  return 1024 + (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * STAGES + 5);
+  return 1024 + (size_t)STAGES * (BM * BK * 2 + BN * BK * 2) + 8 * (2 * STAGES + 6) + sizeof(float) * BN;
 }
 
 template <int BN, int STAGES>
