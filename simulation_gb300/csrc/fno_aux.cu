@@ -54,39 +54,51 @@ __global__ void k_lift_fwd(size_t rows, int C, int cin, const float* __restrict_
 constexpr int kLiftMaxIn = 8;
 
 // The same lift, one thread per (row, 8 channels), 32-bit indices: block
-// (C/8, 256/(C/8)) threads, x = channel group, y = row; the row's inputs are
-// read once per thread and the 8 BF16 results leave as one 16-byte store.
-// Same accumulation order per element as k_lift_fwd, so results are identical.
-__global__ void k_lift_fwd8(int rows, int C, int cin, const float* __restrict__ in, const float* __restrict__ P,
+// (C/8, 256/(C/8)) threads, x = channel group, y = row.  The thread's 8 x CIN
+// weights stay in registers; each iteration loads the inputs of ROWS rows
+// before computing, so several rows' loads are in flight per thread (one row
+// at a time left the kernel waiting on memory latency), and every row leaves
+// as one 16-byte store per thread.  Same accumulation order per element as
+// k_lift_fwd, so results are identical.
+template <int CIN, int ROWS>
+__global__ void k_lift_fwd8(int rows, int C, const float* __restrict__ in, const float* __restrict__ P,
                             const float* __restrict__ p, bf16* __restrict__ x0) {
   const int c0 = threadIdx.x * 8;
-  // this thread's 8 x cin weights and 8 biases stay in registers for all its rows
-  float pv[8], pw[8][kLiftMaxIn];
+  float pv[8], pw[8][CIN];
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     pv[k] = p[c0 + k];
 #pragma unroll
-    for (int j = 0; j < kLiftMaxIn; ++j) pw[k][j] = j < cin ? P[(c0 + k) * cin + j] : 0.f;
+    for (int j = 0; j < CIN; ++j) pw[k][j] = P[(c0 + k) * CIN + j];
   }
-  for (int r = blockIdx.x * blockDim.y + threadIdx.y; r < rows; r += gridDim.x * blockDim.y) {
-    float v[8];
+  const int stride = gridDim.x * blockDim.y;
+  for (int r0 = blockIdx.x * blockDim.y + threadIdx.y; r0 < rows; r0 += ROWS * stride) {
+    float xin[ROWS][CIN];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = pv[k];
+    for (int q = 0; q < ROWS; ++q) {
+      const int r = r0 + q * stride;
 #pragma unroll
-    for (int j = 0; j < kLiftMaxIn; ++j) {
-      if (j < cin) {
-        const float xj = in[(size_t)r * cin + j];
+      for (int j = 0; j < CIN; ++j) xin[q][j] = r < rows ? in[(size_t)r * CIN + j] : 0.f;
+    }
 #pragma unroll
-        for (int k = 0; k < 8; ++k) v[k] = fmaf(pw[k][j], xj, v[k]);
+    for (int q = 0; q < ROWS; ++q) {
+      const int r = r0 + q * stride;
+      if (r >= rows) break;
+      float v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        v[k] = pv[k];
+#pragma unroll
+        for (int j = 0; j < CIN; ++j) v[k] = fmaf(pw[k][j], xin[q][j], v[k]);
       }
-    }
-    uint32_t w[4];
+      uint32_t w[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
-      w[k] = *reinterpret_cast<const uint32_t*>(&h);
+      for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+        w[k] = *reinterpret_cast<const uint32_t*>(&h);
+      }
+      *reinterpret_cast<uint4*>(x0 + (size_t)r * C + c0) = make_uint4(w[0], w[1], w[2], w[3]);
     }
-    *reinterpret_cast<uint4*>(x0 + (size_t)r * C + c0) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
@@ -275,17 +287,29 @@ __global__ void k_dft_to_modes_t(int B, int C, int M, const float* __restrict__ 
   __shared__ float t[kPermSmem];
   const int b = blockIdx.x;
   const int W = 2 * M, n = C * W;
-  const float* src = F + (size_t)b * n;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int c = i / W, j = i - c * W;
-    t[j * (C + 1) + c] = src[i];  // padded row: transposed reads below are conflict-free
+  // read F_b [C][2M] as float4 (W % 4 == 0), scatter into the padded transpose
+  const float4* src = reinterpret_cast<const float4*>(F + (size_t)b * n);
+  for (int i = threadIdx.x; i < n / 4; i += blockDim.x) {
+    const int c = (4 * i) / W, j = 4 * i - c * W;
+    const float4 v = src[i];
+    t[(j + 0) * (C + 1) + c] = v.x;
+    t[(j + 1) * (C + 1) + c] = v.y;
+    t[(j + 2) * (C + 1) + c] = v.z;
+    t[(j + 3) * (C + 1) + c] = v.w;
   }
   __syncthreads();
-  // destination rows: (k, part) -> Fm[k][b][part*C + c], c contiguous
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int j = i / C, c = i - j * C;  // j = part*M + k
+  // destination rows (k, part) -> Fm[k][b][part*C + c .. +7] as 16-byte stores (C % 8 == 0)
+  for (int i = threadIdx.x; i < n / 8; i += blockDim.x) {
+    const int j = (8 * i) / C, c = 8 * i - j * C;  // j = part*M + k
     const int part = j / M, k = j - part * M;
-    Fm[((size_t)k * B + b) * 2 * C + part * C + c] = __float2bfloat16_rn(t[j * (C + 1) + c]);
+    const float* r = t + j * (C + 1) + c;
+    uint32_t w[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const __nv_bfloat162 h2 = __floats2bfloat162_rn(r[2 * e], r[2 * e + 1]);
+      w[e] = *reinterpret_cast<const uint32_t*>(&h2);
+    }
+    *reinterpret_cast<uint4*>(Fm + ((size_t)k * B + b) * 2 * C + part * C + c) = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
@@ -293,16 +317,29 @@ __global__ void k_modes_to_dft_t(int B, int C, int M, const float* __restrict__ 
   __shared__ float t[kPermSmem];
   const int b = blockIdx.x;
   const int W = 2 * M, n = C * W;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int j = i / C, c = i - j * C;  // j = part*M + k
+  // read the 2M mode rows of this sample (C contiguous floats each) as float4
+  for (int i = threadIdx.x; i < n / 4; i += blockDim.x) {
+    const int j = (4 * i) / C, c = 4 * i - j * C;  // j = part*M + k
     const int part = j / M, k = j - part * M;
-    t[j * (C + 1) + c] = Gm[((size_t)k * B + b) * 2 * C + part * C + c];
+    const float4 v = *reinterpret_cast<const float4*>(Gm + ((size_t)k * B + b) * 2 * C + part * C + c);
+    float* r = t + j * (C + 1) + c;
+    r[0] = v.x;
+    r[1] = v.y;
+    r[2] = v.z;
+    r[3] = v.w;
   }
   __syncthreads();
-  bf16* dst = G + (size_t)b * n;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
-    const int c = i / W, j = i - c * W;
-    dst[i] = __float2bfloat16_rn(t[j * (C + 1) + c]);
+  // G_b [C][2M] rows as 16-byte stores (W % 8 == 0)
+  uint4* dst = reinterpret_cast<uint4*>(G + (size_t)b * n);
+  for (int i = threadIdx.x; i < n / 8; i += blockDim.x) {
+    const int c = (8 * i) / W, j = 8 * i - c * W;
+    uint32_t w[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const __nv_bfloat162 h2 = __floats2bfloat162_rn(t[(j + 2 * e) * (C + 1) + c], t[(j + 2 * e + 1) * (C + 1) + c]);
+      w[e] = *reinterpret_cast<const uint32_t*>(&h2);
+    }
+    dst[i] = make_uint4(w[0], w[1], w[2], w[3]);
   }
 }
 
@@ -546,10 +583,12 @@ int fno_lift_fwd(long long rows, int C, int cin, const float* in, const float* P
                  fdtd_stream_t stream) {
   if (!in || !P || !p || !x0) return FDTD_ERR_NULL;
   if (rows < 1 || C < 1 || cin < 1 || cin > fdtd::kLiftMaxIn) return FDTD_ERR_SIZE;
-  if (C % 8 == 0 && C <= 2048 && rows < (1LL << 31) && ((uintptr_t)x0 & 15) == 0) {
+  if ((cin == 2 || cin == 6) && C % 8 == 0 && C <= 2048 && rows < (1LL << 30) && ((uintptr_t)x0 & 15) == 0) {
     const dim3 blk(C / 8, std::max(1, 256 / (C / 8)));
     const long long nblk = std::min<long long>((rows + blk.y - 1) / blk.y, 152LL * 16);
-    FNO_LAUNCH(fdtd::k_lift_fwd8, dim3((unsigned)nblk), blk, (int)rows, C, cin, in, P, p, (bf16*)x0);
+    if (cin == 6)
+      FNO_LAUNCH((fdtd::k_lift_fwd8<6, 4>), dim3((unsigned)nblk), blk, (int)rows, C, in, P, p, (bf16*)x0);
+    FNO_LAUNCH((fdtd::k_lift_fwd8<2, 4>), dim3((unsigned)nblk), blk, (int)rows, C, in, P, p, (bf16*)x0);
   }
   FNO_LAUNCH(fdtd::k_lift_fwd, fdtd::grid1((size_t)rows * C), 256, (size_t)rows, C, cin, in, P, p, (bf16*)x0);
 }
@@ -581,7 +620,8 @@ int fno_cmul(long long n, int nf, const float* P, const float* y, int conj_p, fl
 int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_t stream) {
   if (!F || !Fm) return FDTD_ERR_NULL;
   if (B < 1 || C < 1 || M < 1) return FDTD_ERR_SIZE;
-  if ((C + 1) * 2 * M <= fdtd::kPermSmem)
+  if ((C + 1) * 2 * M <= fdtd::kPermSmem && C % 8 == 0 && M % 4 == 0 && ((uintptr_t)F & 15) == 0 &&
+      ((uintptr_t)Fm & 15) == 0)
     FNO_LAUNCH(fdtd::k_dft_to_modes_t, dim3(B), 256, B, C, M, F, (bf16*)Fm);
   FNO_LAUNCH(fdtd::k_dft_to_modes, fdtd::grid1((size_t)B * C * 2 * M), 256, B, C, M, F, (bf16*)Fm);
 }
@@ -589,7 +629,8 @@ int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_
 int fno_modes_to_dft(int B, int C, int M, const float* Gm, void* G, fdtd_stream_t stream) {
   if (!Gm || !G) return FDTD_ERR_NULL;
   if (B < 1 || C < 1 || M < 1) return FDTD_ERR_SIZE;
-  if ((C + 1) * 2 * M <= fdtd::kPermSmem)
+  if ((C + 1) * 2 * M <= fdtd::kPermSmem && C % 8 == 0 && M % 4 == 0 && ((uintptr_t)Gm & 15) == 0 &&
+      ((uintptr_t)G & 15) == 0)
     FNO_LAUNCH(fdtd::k_modes_to_dft_t, dim3(B), 256, B, C, M, Gm, (bf16*)G);
   FNO_LAUNCH(fdtd::k_modes_to_dft, fdtd::grid1((size_t)B * C * 2 * M), 256, B, C, M, Gm, (bf16*)G);
 }
