@@ -159,7 +159,7 @@ def test_trained_network_gains_over_baselines_and_fdtd(cuda_lib):
     from simulation_gb300 import batch1d as B1
     from simulation_gb300 import surrogate as S
     ntr = 12288
-    X, Y, _ = S.generate_dataset(ntr + 1024, seed=31)
+    X, Y, batch = S.generate_dataset(ntr + 1024, seed=31)
     m = S.FNO(seed=0)
     S.train(m, X[:ntr], Y[:ntr], samples=160_000, batch=256, lr=1e-3, lr_final=1e-4)
     Yte = Y[ntr:]
@@ -174,6 +174,13 @@ def test_trained_network_gains_over_baselines_and_fdtd(cuda_lib):
     assert big.sum() >= 50
     assert np.mean(e_net <= 0.01) >= np.mean(e_zero <= 0.01) + 0.05, (np.mean(e_net <= 0.01), np.mean(e_zero <= 0.01))
     assert np.median(e_net[big]) <= 0.3 * np.median(e_frame[big]), (np.median(e_net[big]), np.median(e_frame[big]))
+    # the damping gate sends the profiles with echo trains to the FDTD: more
+    # spectra end within 1%, and only a minority of profiles is re-solved
+    judge = S.JudgedSurrogate(m, check_frac=0.01, tol=0.01, gate=(1.0, 6.0), seed=0)
+    pred, info = judge(batch.subset(np.arange(ntr, ntr + 1024)), Xd)
+    e_gated = S.rel_l2_spectrum(pred, Yte)
+    assert info["routed"] <= 0.3 * 1024, info["routed"]
+    assert np.mean(e_gated <= 0.01) >= np.mean(e_net <= 0.01) + 0.02, (np.mean(e_gated <= 0.01), np.mean(e_net <= 0.01))
     # throughput of the served path against the batched FDTD (default tuning) on the same distribution
     sps = S.time_inference(m, n=16384, chunk=4096, reps=1)
     r = B1.BatchRunner(B1.slab_batch(4096, seed=32), nsteps=S.NSTEPS, freqs=S.FREQS, wave=S.WAVE)
