@@ -67,9 +67,10 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
   const int g0 = tt * CPT;
 
   // expand the layer table: background ca=1, cb=0.5 (free space of fd1d_1_5).
-  // Cell g = thread*CPT + c is stored at coef[c*T + thread], so the warp's
-  // read of its c-th cells touches consecutive words (a thread-major layout
-  // puts 32 lanes CPT*8 bytes apart: 8-way bank conflicts on every read).
+  // Cell c of thread (warp w, lane l) is stored at coef[(w*CPT + c)*32 + l]:
+  // the warp's read of its c-th cells touches 32 consecutive float2 (a
+  // thread-major layout puts lanes CPT*8 bytes apart: 8-way bank conflicts),
+  // and each thread reads at constant offsets c*256 bytes from its own base.
   const int l0 = p.layer_off[run], l1 = p.layer_off[run + 1];
   for (int i = tt; i < T * CPT; i += T) {
     float ca = 1.f, cb = 0.5f;
@@ -78,8 +79,10 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
         ca = p.layer_ca[l];
         cb = p.layer_cb[l];
       }
-    coef[(i % CPT) * T + i / CPT] = make_float2(ca, cb);
+    const int th = i / CPT, c = i - th * CPT;
+    coef[((th >> 5) * CPT + c) * 32 + (th & 31)] = make_float2(ca, cb);
   }
+  const float2* my_coef = coef + (size_t)w * CPT * 32 + lane;
   const int pin = p.probe_in[run], pout = p.probe_out[run];
   const int nf = p.nf;
   // DFT accumulators of the team in shared memory: acc[4][nf] (re/im at the
@@ -115,7 +118,7 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
       const int g = g0 + c;
       const float hym = (c == 0) ? hy_left : hy[c - 1];
       if (g >= 1 && g < nx) {
-        const float2 k = coef[c * T + tt];
+        const float2 k = my_coef[c * 32];
         ex[c] = ex_update_cacb(ex[c], hym, hy[c], k.x, k.y);
       }
       if (g == p.src_k) ex[c] = __fadd_rn(ex[c], v);  // soft source, fd1d/program/fd1d_1_5.py:67
