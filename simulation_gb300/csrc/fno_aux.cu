@@ -587,8 +587,8 @@ int fno_lift_fwd(long long rows, int C, int cin, const float* in, const float* P
     const dim3 blk(C / 8, std::max(1, 256 / (C / 8)));
     const long long nblk = std::min<long long>((rows + blk.y - 1) / blk.y, 152LL * 16);
     if (cin == 6)
-      FNO_LAUNCH((fdtd::k_lift_fwd8<6, 4>), dim3((unsigned)nblk), blk, (int)rows, C, in, P, p, (bf16*)x0);
-    FNO_LAUNCH((fdtd::k_lift_fwd8<2, 4>), dim3((unsigned)nblk), blk, (int)rows, C, in, P, p, (bf16*)x0);
+      FNO_LAUNCH((fdtd::k_lift_fwd8<6, 8>), dim3((unsigned)nblk), blk, (int)rows, C, in, P, p, (bf16*)x0);
+    FNO_LAUNCH((fdtd::k_lift_fwd8<2, 8>), dim3((unsigned)nblk), blk, (int)rows, C, in, P, p, (bf16*)x0);
   }
   FNO_LAUNCH(fdtd::k_lift_fwd, fdtd::grid1((size_t)rows * C), 256, (size_t)rows, C, cin, in, P, p, (bf16*)x0);
 }

@@ -17,7 +17,8 @@
 //     overlap a tile's epilogue with the next tile's MMAs.  Eight epilogue
 //     warps (two per SM sub-partition) rather than four: with four, the
 //     pointwise layer's GEMM (K = 192) spent most of its time in the
-//     epilogue and moved 3.6 TB/s.
+//     epilogue and moved 3.6 TB/s; with eight it moves about 4.7 TB/s, and
+//     sixteen (one 32-column chunk each) measured no faster.
 // Operands may be K-major or MN-major (the transposed products of the
 // backward pass need MN-major), selected per call.  Every wait on an mbarrier
 // is bounded (about 2 s): on expiry the kernel records FDTD_STATUS_TIMEOUT in
@@ -315,7 +316,11 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int col0 = n0 + c0;
         float z[32];
   #pragma unroll
-        for (int q = 0; q < 32; ++q) z[q] = __fmul_rn(a.alpha, __uint_as_float(r[q]));
+        for (int q = 0; q < 32; ++q) z[q] = __uint_as_float(r[q]);
+        if (a.alpha != 1.0f) {  // alpha = 1 (every surrogate product): no multiply, the same values
+  #pragma unroll
+          for (int q = 0; q < 32; ++q) z[q] = __fmul_rn(a.alpha, z[q]);
+        }
         if (a.bias) {
           const float* bsrc = bias_smem ? sbias + c0 : a.bias + col0;
   #pragma unroll
