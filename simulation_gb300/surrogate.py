@@ -343,7 +343,7 @@ class FNO:
         outs = [self.forward(inp[i:i + chunk]) for i in range(0, inp.shape[0], chunk)]
         return torch.cat(outs) if len(outs) > 1 else outs[0]
 
-    def spectrum(self, inp: torch.Tensor, chunk: int = 4096, streams: int = 2) -> torch.Tensor:
+    def spectrum(self, inp: torch.Tensor, chunk: int = 4096, streams: int = 3) -> torch.Tensor:
         """Predicted transmission [B][2*NFREQ] = [Re T | Im T] = P (.) y.
 
         Chunks alternate between ``streams`` CUDA streams, so that one chunk's
