@@ -279,6 +279,16 @@ int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_
 int fno_modes_to_dft(int B, int C, int M, const float* Gm, void* G, fdtd_stream_t stream);
 int fno_build_rbig(int M, int C, const float* Rr, const float* Ri, void* Rbig, fdtd_stream_t stream);
 int fno_fold_drbig(int M, int C, const float* dRbig, float* dRr, float* dRi, fdtd_stream_t stream);
+/* Inference with the lift folded into the first spectral layer (the lift is
+ * linear): inputs [B][N][cin] packed as BF16 rows (features, 1, zeros) into
+ * out [B][N][ldo] (ldo >= 16, multiple of 8; columns 16.. are zeroed only if
+ * write_pad) and, if out_t is not NULL, into out_t [N][B][16]; FP32
+ * C[b] = A[b].B for the folded weights; rectangular complex-weight expansion
+ * Rbig [M][2Co][2Ci] from Rr, Ri [M][Co][Ci]. */
+int fno_pack_inputs(int B, int N, int cin, int ldo, int write_pad, const float* in, void* out, void* out_t,
+                    fdtd_stream_t stream);
+int fno_small_matmul(int batch, int M, int N, int K, const float* A, const float* B, float* C, fdtd_stream_t stream);
+int fno_build_rbig_rect(int M, int Co, int Ci, const float* Rr, const float* Ri, void* Rbig, fdtd_stream_t stream);
 int fno_gelu_fwd(long long n, const float* z, void* y, void* pre, fdtd_stream_t stream);
 int fno_gelu_bwd(long long n, const void* dy16, const float* dy32, const void* pre, void* dz, fdtd_stream_t stream);
 int fno_meanpool(int B, int N, int C, const void* x, void* h, fdtd_stream_t stream);

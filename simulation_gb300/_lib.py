@@ -146,6 +146,9 @@ _SIGS = {
     "fno_modes_to_dft": ([C.c_int, C.c_int, C.c_int, F, P, P], C.c_int),
     "fno_build_rbig": ([C.c_int, C.c_int, F, F, P, P], C.c_int),
     "fno_fold_drbig": ([C.c_int, C.c_int, F, F, F, P], C.c_int),
+    "fno_pack_inputs": ([C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, F, P, P, P], C.c_int),
+    "fno_small_matmul": ([C.c_int, C.c_int, C.c_int, C.c_int, F, F, F, P], C.c_int),
+    "fno_build_rbig_rect": ([C.c_int, C.c_int, C.c_int, F, F, P, P], C.c_int),
     "fno_gelu_fwd": ([C.c_longlong, F, P, P, P], C.c_int),
     "fno_gelu_bwd": ([C.c_longlong, P, F, P, P, P], C.c_int),
     "fno_meanpool": ([C.c_int, C.c_int, C.c_int, P, P, P], C.c_int),

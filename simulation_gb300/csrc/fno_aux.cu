@@ -386,6 +386,73 @@ __global__ void k_build_rbig(int M, int C, const float* __restrict__ Rr, const f
   }
 }
 
+// Rectangular Rbig for the folded first layer: Rr, Ri are [M][Co][Ci],
+// Rbig [M][2Co][2Ci] = [[Rr, -Ri], [Ri, Rr]]
+__global__ void k_build_rbig_rect(int M, int Co, int Ci, const float* __restrict__ Rr, const float* __restrict__ Ri,
+                                  bf16* __restrict__ Rbig) {
+  const size_t total = (size_t)M * 4 * Co * Ci;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int col = (int)(i % (2 * Ci));
+    const int row = (int)((i / (2 * Ci)) % (2 * Co));
+    const int k = (int)(i / (4 * (size_t)Co * Ci));
+    const int ro = row % Co, co = col % Ci;
+    const size_t s = ((size_t)k * Co + ro) * Ci + co;
+    float v;
+    if (row < Co) v = (col < Ci) ? Rr[s] : -Ri[s];
+    else v = (col < Ci) ? Ri[s] : Rr[s];
+    Rbig[i] = __float2bfloat16_rn(v);
+  }
+}
+
+// C[b] = A[b] . B in FP32 (row-major, B shared), one thread per output: the
+// small weight products of the folded first layer (W0 P', R_k P')
+__global__ void k_small_matmul(int batch, int M, int N, int K, const float* __restrict__ A, const float* __restrict__ B,
+                               float* __restrict__ Cm) {
+  const size_t total = (size_t)batch * M * N;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int n = (int)(i % N);
+    const size_t bm = i / N;
+    const float* a = A + bm * K;
+    float t = 0.f;
+    for (int k = 0; k < K; ++k) t = fmaf(a[k], B[(size_t)k * N + n], t);
+    Cm[i] = t;
+  }
+}
+
+// inputs for the folded first layer, one thread per row (b, n): the row
+// (bf16(in[b][n][0..cin-1]), 1, 0 ... 0) goes to out[b][n][0..ldo-1]
+// (sample-major, for the pointwise product; 64 wide, because narrower rows
+// make the GEMM's TMA loads of A slow: 1.5 ms at K = 16 against 0.83 ms at
+// K = 64 for 4096 spectra) and, when outT is given, to outT[n][b][0..15]
+// (position-major, so the DFT of every sample's channels is one GEMM with the
+// samples along M)
+__global__ void k_pack_inputs16(int B, int N, int cin, int ldo, int write_pad, const float* __restrict__ in,
+                                bf16* __restrict__ out, bf16* __restrict__ outT) {
+  const long long rows = (long long)B * N;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < rows; r += (long long)gridDim.x * blockDim.x) {
+    const int b = (int)(r / N), n = (int)(r - (long long)b * N);
+    uint32_t w[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int j0 = 2 * k, j1 = 2 * k + 1;
+      const float v0 = j0 < cin ? in[r * cin + j0] : (j0 == cin ? 1.0f : 0.0f);
+      const float v1 = j1 < cin ? in[r * cin + j1] : (j1 == cin ? 1.0f : 0.0f);
+      const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+      w[k] = *reinterpret_cast<const uint32_t*>(&h);
+    }
+    uint4* o = reinterpret_cast<uint4*>(out + r * ldo);
+    o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    if (write_pad)  // a caller reusing a zeroed buffer skips the constant padding
+      for (int k = 2; k < ldo / 8; ++k) o[k] = make_uint4(0u, 0u, 0u, 0u);
+    if (outT) {
+      uint4* t = reinterpret_cast<uint4*>(outT + ((long long)n * B + b) * 16);
+      t[0] = make_uint4(w[0], w[1], w[2], w[3]);
+      t[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    }
+  }
+}
+
 __global__ void k_fold_drbig(int M, int C, const float* __restrict__ dRbig, float* __restrict__ dRr,
                              float* __restrict__ dRi) {
   const size_t total = (size_t)M * C * C;
@@ -639,6 +706,27 @@ int fno_build_rbig(int M, int C, const float* Rr, const float* Ri, void* Rbig, f
   if (!Rr || !Ri || !Rbig) return FDTD_ERR_NULL;
   if (M < 1 || C < 1) return FDTD_ERR_SIZE;
   FNO_LAUNCH(fdtd::k_build_rbig, fdtd::grid1((size_t)M * 4 * C * C), 256, M, C, Rr, Ri, (bf16*)Rbig);
+}
+
+int fno_build_rbig_rect(int M, int Co, int Ci, const float* Rr, const float* Ri, void* Rbig, fdtd_stream_t stream) {
+  if (!Rr || !Ri || !Rbig) return FDTD_ERR_NULL;
+  if (M < 1 || Co < 1 || Ci < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_build_rbig_rect, fdtd::grid1((size_t)M * 4 * Co * Ci), 256, M, Co, Ci, Rr, Ri, (bf16*)Rbig);
+}
+
+int fno_small_matmul(int batch, int M, int N, int K, const float* A, const float* B, float* Cm, fdtd_stream_t stream) {
+  if (!A || !B || !Cm) return FDTD_ERR_NULL;
+  if (batch < 1 || M < 1 || N < 1 || K < 1) return FDTD_ERR_SIZE;
+  FNO_LAUNCH(fdtd::k_small_matmul, fdtd::grid1((size_t)batch * M * N), 256, batch, M, N, K, A, B, Cm);
+}
+
+int fno_pack_inputs(int B, int N, int cin, int ldo, int write_pad, const float* in, void* out, void* out_t,
+                    fdtd_stream_t stream) {
+  if (!in || !out) return FDTD_ERR_NULL;
+  if (B < 1 || N < 1 || cin < 1 || cin > 15 || ldo < 16 || ldo % 8) return FDTD_ERR_SIZE;
+  if (((uintptr_t)out & 15) || ((uintptr_t)out_t & 15)) return FDTD_ERR_ALIGN;
+  FNO_LAUNCH(fdtd::k_pack_inputs16, fdtd::grid1((size_t)B * N), 256, B, N, cin, ldo, write_pad, in, (bf16*)out,
+             (bf16*)out_t);
 }
 
 int fno_fold_drbig(int M, int C, const float* dRbig, float* dRr, float* dRi, fdtd_stream_t stream) {

@@ -559,9 +559,10 @@ extern "C" int fdtd_gemm_bf16(const fdtd_gemm_desc* d, int* status, fdtd_stream_
   g.a_shared = a_sh ? 1 : 0;
   g.b_shared = b_sh ? 1 : 0;
   g.status = status;
-  const bool deep = d->K + g.K2 > 2 * BK;  // pipeline depth: 4 stages for long K, 2 for short K
+  // 4 pipeline stages throughout: with 2, a product of only one or two
+  // k-blocks per tile (K = 16 + 64 in the folded first layer) cannot load the
+  // next tile while the current one computes (1.6 ms instead of 0.9 at 4096)
   cudaStream_t st = (cudaStream_t)stream;
-  if (BN == 64)
-    return deep ? launch_gemm_t<64, 4>(ta, tb, ta2, tb2, g, st) : launch_gemm_t<64, 2>(ta, tb, ta2, tb2, g, st);
-  return deep ? launch_gemm_t<128, 4>(ta, tb, ta2, tb2, g, st) : launch_gemm_t<128, 2>(ta, tb, ta2, tb2, g, st);
+  if (BN == 64) return launch_gemm_t<64, 4>(ta, tb, ta2, tb2, g, st);
+  return launch_gemm_t<128, 4>(ta, tb, ta2, tb2, g, st);
 }

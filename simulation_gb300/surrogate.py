@@ -163,6 +163,7 @@ class FNO:
         self.dev = torch.device(device)
         self.N, self.C, self.M, self.L, self.H, self.D = nbins, width, modes, layers, hidden, out
         self.cin = cin
+        self.fold = True  # inference folds the lift into the first layer (see _refresh_folded)
         g = torch.Generator().manual_seed(seed)
         C, M, H, D = width, modes, hidden, out
 
@@ -202,6 +203,63 @@ class FNO:
             _call("fno_build_rbig", self.M, self.C, self.p[f"L{l}.Rr"].data_ptr(), self.p[f"L{l}.Ri"].data_ptr(),
                   t.data_ptr())
             self.rbig.append(t)
+        self._folded_stale = True  # rebuilt by the next inference forward
+
+    # ------------------------------------------------------------ folded first layer (inference)
+    KIN = 16  # packed input width of the DFT operand: cin features, a constant 1, zeros
+    KPW = 64  # the pointwise operand is packed 64 wide (128-byte rows load fast through TMA)
+
+    def _refresh_folded(self):
+        """The lift x0 = in P^T + p is linear, so inference can skip it: with
+        P' = [P | p | 0] ([C][KIN]) and inputs (features, 1, 0...), the first
+        layer's pointwise weight becomes W0 P' and its complex mode weights
+        R_k P' (FP32 products on the device, then BF16).  The first layer then
+        reads 16 input channels instead of a 128-channel activation."""
+        C, M, KIN = self.C, self.M, self.KIN
+        self._folded_stale = False
+        KPW = self.KPW
+        Pw = torch.zeros((C, KPW), dtype=torch.float32, device=self.dev)  # assembled by copies
+        Pw[:, :self.cin].copy_(self.p["P"])
+        Pw[:, self.cin].copy_(self.p["pb"])
+        Pp = Pw[:, :KIN].contiguous()
+        w0 = torch.empty((C, KPW), dtype=torch.float32, device=self.dev)
+        _call("fno_small_matmul", 1, C, KPW, C, self.p["L0.W"].data_ptr(), Pw.data_ptr(), w0.data_ptr())
+        self.w0f16 = torch.empty((C, KPW), dtype=BF, device=self.dev)
+        _call("fno_to_bf16", w0.numel(), w0.data_ptr(), self.w0f16.data_ptr())
+        rr = torch.empty((M, C, KIN), dtype=torch.float32, device=self.dev)
+        ri = torch.empty((M, C, KIN), dtype=torch.float32, device=self.dev)
+        _call("fno_small_matmul", M, C, KIN, C, self.p["L0.Rr"].data_ptr(), Pp.data_ptr(), rr.data_ptr())
+        _call("fno_small_matmul", M, C, KIN, C, self.p["L0.Ri"].data_ptr(), Pp.data_ptr(), ri.data_ptr())
+        self.rbig0f = torch.empty((M, 2 * C, 2 * KIN), dtype=BF, device=self.dev)
+        _call("fno_build_rbig_rect", M, C, KIN, rr.data_ptr(), ri.data_ptr(), self.rbig0f.data_ptr())
+
+    def _first_layer_folded(self, inp: torch.Tensor, phi_b: torch.Tensor) -> torch.Tensor:
+        """x1 of the first spectral layer straight from the packed inputs."""
+        Bn, N, C, M, KIN = inp.shape[0], self.N, self.C, self.M, self.KIN
+        dev = self.dev
+        # the 64-wide operand lives per (stream, batch size): its zero padding is
+        # written once, and each call rewrites only the 16 live columns
+        key = (torch.cuda.current_stream(dev).cuda_stream, Bn)
+        if not hasattr(self, "_packed"):
+            self._packed = {}
+        inp16 = self._packed.get(key)
+        if inp16 is None:
+            inp16 = torch.zeros((Bn, N, self.KPW), dtype=BF, device=dev)
+            self._packed[key] = inp16
+        inpT = torch.empty((N, Bn * KIN), dtype=BF, device=dev)  # position-major copy
+        _call("fno_pack_inputs", Bn, N, self.cin, self.KPW, 0, inp.data_ptr(), inp16.data_ptr(), inpT.data_ptr())
+        # the DFT of every sample's 16 channels in one product: F[(b, c)][j] = sum_n inpT[n][(b, c)] Phi[j][n]
+        F = torch.empty((Bn, KIN, 2 * M), dtype=torch.float32, device=dev)
+        gemm(inpT, self.phi16, a_mn=True, out=F.view(Bn * KIN, 2 * M))
+        Fm = torch.empty((M, Bn, 2 * KIN), dtype=BF, device=dev)
+        _call("fno_dft_to_modes", Bn, KIN, M, F.data_ptr(), Fm.data_ptr())
+        Gm = torch.empty((M, Bn, 2 * C), dtype=torch.float32, device=dev)
+        gemm(Fm, self.rbig0f, out=Gm)
+        G = torch.empty((Bn, C, 2 * M), dtype=BF, device=dev)
+        _call("fno_modes_to_dft", Bn, C, M, Gm.data_ptr(), G.data_ptr())
+        x = torch.empty((Bn, N, C), dtype=BF, device=dev)
+        gemm(inp16, self.w0f16, out=x, bias=self.p["L0.b"], gelu=True, second=(self.psi16, G, False, False))
+        return x
 
     def state_dict(self):
         return {k: v.detach().cpu().clone() for k, v in self.p.items()}
@@ -216,16 +274,22 @@ class FNO:
         """inp [B][N][cin] float32 (device) -> network output y [B][D] float32."""
         Bn, N, C, M = inp.shape[0], self.N, self.C, self.M
         dev = self.dev
-        x = torch.empty((Bn, N, C), dtype=BF, device=dev)
-        _call("fno_lift_fwd", Bn * N, C, self.cin, inp.data_ptr(), self.p["P"].data_ptr(), self.p["pb"].data_ptr(),
-              x.data_ptr())
+        phi_b = self.phi16.unsqueeze(0).expand(Bn, -1, -1)  # stride 0 over the batch
+        folded = not keep and self.fold and self.cin + 1 <= self.KIN
+        if folded:
+            if self._folded_stale:
+                self._refresh_folded()
+            x = self._first_layer_folded(inp, phi_b)
+        else:
+            x = torch.empty((Bn, N, C), dtype=BF, device=dev)
+            _call("fno_lift_fwd", Bn * N, C, self.cin, inp.data_ptr(), self.p["P"].data_ptr(),
+                  self.p["pb"].data_ptr(), x.data_ptr())
         saved = {"inp": inp, "x": [], "pre": [], "Fm": []}
         F = torch.empty((Bn, C, 2 * M), dtype=torch.float32, device=dev)
         Fm = torch.empty((M, Bn, 2 * C), dtype=BF, device=dev)
         Gm = torch.empty((M, Bn, 2 * C), dtype=torch.float32, device=dev)
         G = torch.empty((Bn, C, 2 * M), dtype=BF, device=dev)
-        phi_b = self.phi16.unsqueeze(0).expand(Bn, -1, -1)  # stride 0 over the batch
-        for l in range(self.L):
+        for l in range(1 if folded else 0, self.L):
             # truncated DFT: F_b[C][2M] = x_b^T Phi^T   (A = x_b stored [N][C]: MN-major)
             gemm(x, phi_b, a_mn=True, out=F)
             _call("fno_dft_to_modes", Bn, C, M, F.data_ptr(), Fm.data_ptr())
@@ -349,7 +413,10 @@ class FNO:
         Chunks alternate between ``streams`` CUDA streams, so that one chunk's
         lighter kernels (permutes, frame, head) overlap another's GEMMs."""
         main = torch.cuda.current_stream(self.dev)
-        _wdt_table(inp.device)  # made on the caller's stream, before any side stream reads it
+        # shared tables are made on the caller's stream, before any side stream reads them
+        _wdt_table(inp.device)
+        if self.fold and self._folded_stale and self.cin + 1 <= self.KIN:
+            self._refresh_folded()
         nchunk = -(-inp.shape[0] // chunk)
         if nchunk == 1 or streams <= 1:
             outs = [cmul(propagation(inp[i:i + chunk]), self.forward(inp[i:i + chunk]))

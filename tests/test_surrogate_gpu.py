@@ -69,6 +69,30 @@ def test_gradients_in_frame_with_relative_loss(cuda_lib):
     assert not bad, f"gradient rel-L2 above 6e-2: {bad}"
 
 
+def test_folded_first_layer_matches_the_lift(cuda_lib):
+    """Inference folds the linear lift into the first layer's weights; the
+    outputs match the unfolded forward within the BF16 rounding of either."""
+    from simulation_gb300 import batch1d as B1
+    from simulation_gb300 import surrogate as S
+    m = S.FNO(seed=3)
+    g = torch.Generator().manual_seed(5)
+    m.p["H2"].copy_(((torch.rand(m.p["H2"].shape, generator=g) * 2 - 1) / 16).cuda())
+    m.p["hb2"].copy_(((torch.rand(m.p["hb2"].shape, generator=g) * 2 - 1) / 10).cuda())
+    m._refresh_bf16()
+    inp = torch.as_tensor(S.profile_features(B1.slab_batch(24, seed=9))).cuda()
+    m.fold = False
+    ref = m.forward(inp).double()
+    m.fold = True
+    out = m.forward(inp).double()
+    torch.cuda.synchronize()
+    assert float((out - ref).norm() / ref.norm()) <= 2e-2
+    # and the served path (three streams, several chunks) gives the same spectra as one chunk
+    s1 = m.spectrum(inp, chunk=24, streams=1)
+    s3 = m.spectrum(inp, chunk=8, streams=3)
+    torch.cuda.synchronize()
+    assert torch.equal(s1, s3)
+
+
 def test_cmul_matches_complex_product(cuda_lib):
     from simulation_gb300 import surrogate as S
     g = torch.Generator().manual_seed(4)
