@@ -277,6 +277,10 @@ def run_ours(args) -> None:
         cpu = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS", "150")))
         cpu["unit"] = UNIT
         cpu["kind"] = "port"
+        one = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS_1T", "10")), threads=1)
+        cpu["single_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
+        from oracle import ccore
+        ccore.lib32().oracle_set_threads(cpu["cores"])
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -302,7 +306,7 @@ def run_secondary(args, st, world) -> dict:
     """The other workloads of the path, measured after the headline (not part of `value`)."""
     import torch
     out = {"fd1d_dielectric_ke200_1000steps": _bench_fd1d(st)}
-    batch = _bench_batch1d(st)
+    batch = _bench_batch1d(st, cpu=not args.no_cpu)
     out["batch1d_4096_slabs_8000steps"] = batch
     out["fd2d_tfsf_dft_2048sq"] = _bench_tfsf_dft(st)
     out["adjoint_1024sq_3000steps"] = _bench_adjoint(st)
@@ -358,7 +362,7 @@ def _bench_fd1d(st, reps: int = 20) -> dict:
     return {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3, "kernel_launches_per_run": 1}
 
 
-def _bench_batch1d(st, nruns: int = 4096, autotune: bool = True) -> dict:
+def _bench_batch1d(st, nruns: int = 4096, autotune: bool = True, cpu: bool = False) -> dict:
     """Batched uneven 1D slab runs: ke ~ U[500,20000], 8000 steps, 64-frequency probes."""
     import torch
 
@@ -375,9 +379,34 @@ def _bench_batch1d(st, nruns: int = 4096, autotune: bool = True) -> dict:
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     cells = int(batch.ke.sum()) * 8000
-    return {"ms": ms, "Gcell_updates_per_s": cells / ms / 1e6, "spectra_per_s": batch.nruns / ms * 1e3,
-            "tuning": tuned["tuning"], "status": int(runner.status.item()),
-            "runs_done": int(runner.done.sum().item())}
+    res = {"ms": ms, "Gcell_updates_per_s": cells / ms / 1e6, "spectra_per_s": batch.nruns / ms * 1e3,
+           "tuning": tuned["tuning"], "status": int(runner.status.item()),
+           "runs_done": int(runner.done.sum().item())}
+    if cpu:
+        res["cpu_baseline"] = _cpu_batch1d(batch, runner)
+    return res
+
+
+def _cpu_batch1d(batch, runner, nsample: int = 64) -> dict:
+    """The same runs in the C port of the per-run loop (float32, one run per
+    OpenMP thread, all host cores) on a seeded sample of the batch."""
+    import numpy as np
+
+    from oracle import ccore
+    from simulation_gb300 import batch1d as B
+    idx = np.random.default_rng(0).choice(batch.nruns, size=min(nsample, batch.nruns), replace=False)
+    b = batch.subset(idx)
+    lca, lcb = B.layer_coeffs(b.epsr, b.sigma)
+    ns = runner.nsteps
+    lib = ccore.lib32()
+    t0 = time.perf_counter()
+    ccore.fd1d_batch(lib, np.float32, b.ke, b.layer_off, b.layer_start, b.layer_end, lca, lcb, b.src_k,
+                     runner.src_table.double().cpu().numpy()[:ns], ns, runner.dft_cos.double().cpu().numpy()[:ns],
+                     runner.dft_sin.double().cpu().numpy()[:ns], b.probe_in, b.probe_out)
+    el = time.perf_counter() - t0
+    return {"Gcell_updates_per_s": float(b.ke.sum()) * ns / el / 1e9, "spectra_per_s": b.nruns / el,
+            "cores": int(lib.oracle_threads()), "kind": "port",
+            "sample": f"{b.nruns} runs of the batch, {ns} steps (float32 C port, OpenMP over runs)"}
 
 
 def _bench_adjoint(st) -> dict:
