@@ -146,7 +146,9 @@ int fdtd2d_hxinct(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream)
 int fdtd2d_incth(const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
 int fdtd2d_fourier(int t, const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t stream);
 
-/* Bytes of device workspace fdtd2d_step_n needs for these params (0 if none). */
+/* Bytes of device workspace fdtd2d_step_n needs for these params (0 if none):
+ * the ping-pong field copies, plus 64 incident-line rows of ny floats with
+ * TF/SF on. */
 size_t fdtd2d_workspace_size(const fdtd2d_params* p, int steps_per_pass);
 
 /* fdtd2d_step_n: the program's time loop for t = t0+1 .. t0+nsteps, in the
@@ -156,9 +158,14 @@ size_t fdtd2d_workspace_size(const fdtd2d_params* p, int steps_per_pass);
  * pass over HBM; `workspace` (fdtd2d_workspace_size bytes, 256-byte aligned)
  * holds the ping-pong copy of the evolving fields.  Results land in the
  * caller's arrays, bitwise equal to calling dfield/efield/hfield per step.
- * With TF/SF or DFT enabled each step runs as three launches (D + ezinct +
- * inctdz; E + fourier + hxinct; H + incthx + incthy), bitwise equal to the nine
- * per-function calls.
+ * TF/SF and the running DFT (nf <= 8) ride in the same fused passes: the
+ * incident line is advanced ahead of them in one launch per 64 steps (its
+ * tables are part of the workspace), the box-edge corrections and the DFT
+ * accumulation happen inside the pass, bitwise equal to the nine per-function
+ * calls per step.  Grids with ny % 4 != 0, nf > 8, TF/SF with ny > 16384, a
+ * probe trace together with TF/SF or the DFT, or nsteps == 1 run each step as
+ * three launches instead (D + ezinct + inctdz; E + fourier + hxinct; H +
+ * incthx + incthy; no workspace), with the same results.
  * Replaces the `for t in 1..ns` loops of fd2d/python/fd2d_3_2.py:139-142 and
  * fd2d/cuda/fd2d_3_4.cu:327-336. */
 int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass,
@@ -179,7 +186,8 @@ int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows
  * first call on a device looks the array's address up (cudaGetSymbolAddress):
  * make it before any stream capture.  All calls share the array (it keeps the
  * last call's contents, none of which must start at zero); calls that overlap
- * on the GPU race on it. */
+ * on the GPU race on it.  With TF/SF or the DFT on and a workspace larger than
+ * the array, each step is one fdtd2d_step_n call of one step instead. */
 #define FDTD2D_NOALLOC_MAX_CELLS (1024 * 1024)
 #define FDTD2D_NOALLOC_SCRATCH_BYTES (6ull * 4ull * FDTD2D_NOALLOC_MAX_CELLS)
 int fdtd2d_step_n_noalloc(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass,

@@ -49,9 +49,19 @@ int check_params(const fdtd2d_params* p, const fdtd2d_state* s, int t_last, bool
   return FDTD_OK;
 }
 
-bool fused_ok(const fdtd2d_params* p, const fdtd2d_state* s) {
-  if (p->tfsf_npml > 0 || p->nf > 0) return false;
+bool ext_on(const fdtd2d_params* p) { return p->tfsf_npml > 0 || p->nf > 0; }
+
+// what the fused path needs of the parameters alone (the workspace query
+// sees only these)
+bool fused_params_ok(const fdtd2d_params* p) {
   if (p->ny % 4 != 0) return false;
+  return !ext_on(p) || march_ext_supported(*p);
+}
+
+bool fused_ok(const fdtd2d_params* p, const fdtd2d_state* s) {
+  if (!fused_params_ok(p)) return false;
+  if (ext_on(p) && s->probe_ez) return false;  // the probe trace is kept by the plain kernels only
+  if (p->nf > 0 && (!aligned16(s->r_pt) || !aligned16(s->i_pt))) return false;
   const void* ptrs[] = {s->dz, s->ez, s->hx, s->hy, p->naz};
   for (const void* q : ptrs)
     if (!aligned16(q)) return false;
@@ -66,6 +76,16 @@ size_t slot_bytes(const fdtd2d_params* p) {
 }
 
 int nslots(const fdtd2d_params* p) { return 3 + (p->nbz ? 1 : 0) + (has_pml(*p) ? 2 : 0); }
+
+size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+// incident-line tables of one chunk of steps (TF/SF): inc_e [chunk][ny],
+// inc_h [chunk][2]
+size_t line_e_bytes(const fdtd2d_params* p) { return round256((size_t)kLineChunkSteps * p->ny * sizeof(float)); }
+size_t line_bytes(const fdtd2d_params* p) {
+  return p->tfsf_npml > 0 ? line_e_bytes(p) + round256((size_t)kLineChunkSteps * 2 * sizeof(float)) : 0;
+}
+size_t fused_workspace_bytes(const fdtd2d_params* p) { return slot_bytes(p) * nslots(p) + line_bytes(p); }
 
 // one time step in the reference's order (fd2d/python/fd2d_3_4.py:268-277):
 // ezinct, dfield, inctdz, efield, fourier, hxinct, hfield, incthx, incthy in
@@ -145,8 +165,8 @@ int fdtd2d_fourier(int t, const fdtd2d_params* p, fdtd2d_state* s, fdtd_stream_t
 size_t fdtd2d_workspace_size(const fdtd2d_params* p, int steps_per_pass) {
   (void)steps_per_pass;
   if (!p || p->nx < 3 || p->ny < 3) return 0;
-  if (p->tfsf_npml > 0 || p->nf > 0 || p->ny % 4 != 0) return 0;
-  return slot_bytes(p) * nslots(p);
+  if (!fused_params_ok(p)) return 0;
+  return fused_workspace_bytes(p);
 }
 
 int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, int steps_per_pass, void* workspace,
@@ -165,7 +185,7 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
     return fdtd_host::check_launch();
   }
 
-  const size_t need = slot_bytes(p) * nslots(p);
+  const size_t need = fused_workspace_bytes(p);
   if (!workspace || workspace_bytes < need) return FDTD_ERR_WORKSPACE;
   if (((uintptr_t)workspace & 255u) != 0) return FDTD_ERR_ALIGN;
 
@@ -210,11 +230,47 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
       ws.ihy = (float*)(base + sb * k++);
     }
   }
+  MarchExt ext{};
+  float* inc_e = nullptr;
+  float* inc_h = nullptr;
+  if (ext_on(p)) {
+    ext.tfsf_npml = p->tfsf_npml;
+    ext.nf = p->nf;
+    ext.dft_cos = p->dft_cos;
+    ext.dft_sin = p->dft_sin;
+    ext.r_pt = s->r_pt;
+    ext.i_pt = s->i_pt;
+    if (p->tfsf_npml > 0) {
+      char* lb = (char*)workspace + slot_bytes(p) * nslots(p);
+      inc_e = (float*)lb;
+      inc_h = (float*)(lb + line_e_bytes(p));
+    }
+    // (without TF/SF no warp runs the edge logic that reads the tables)
+    ext.inc_e = inc_e;
+    ext.inc_h = inc_h;
+  }
   int t = t0;
+  int line_t0 = t0, line_n = 0;  // steps the incident-line tables hold
   for (size_t i = 0; i < sched.size(); ++i) {
     const FieldSet& in = (i % 2 == 0) ? user : ws;
     const FieldSet& out = (i % 2 == 0) ? ws : user;
-    if ((rc = launch_march(*p, in, out, s->ez, t, sched[i], s->status, s->probe_ez, st))) return rc;
+    if (!ext_on(p)) {
+      rc = launch_march(*p, in, out, s->ez, t, sched[i], s->status, s->probe_ez, st);
+    } else {
+      if (p->tfsf_npml > 0) {
+        if (t + sched[i] > line_t0 + line_n) {  // next chunk of whole passes
+          int n = 0;
+          for (size_t q = i; q < sched.size() && n + sched[q] <= kLineChunkSteps; ++q) n += sched[q];
+          if ((rc = launch_inc_line(*p, *s, t, n, inc_e, inc_h, st))) return rc;
+          line_t0 = t;
+          line_n = n;
+        }
+        ext.inc_e = inc_e + (size_t)(t - line_t0) * p->ny;
+        ext.inc_h = inc_h + (size_t)(t - line_t0) * 2;
+      }
+      rc = launch_march_ext(*p, in, out, s->ez, t, sched[i], s->status, ext, st);
+    }
+    if (rc) return rc;
     t += sched[i];
   }
   if (copy_back) {

@@ -37,4 +37,34 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
 // columns a warp of the fused kernel owns (for workspace/grid sizing)
 int march_max_steps_per_pass();
 
+// The fd2d_3_4 extras inside a fused pass (fd2d/python/fd2d_3_4.py:90-170):
+// the TF/SF box corrections (inctdz, incthx, incthy) from a precomputed
+// incident line, and the running DFT of Ez at every cell.
+struct MarchExt {
+  int tfsf_npml;       // 0: no TF/SF
+  const float* inc_e;  // [k][ny]: ezi after step t0+s+1's ezinct and source (row s)
+  const float* inc_h;  // [k][2]: hxi[npml-2], hxi[ny-npml] before step t0+s+1's hxinct
+  int nf;              // 0: no DFT
+  const float* dft_cos;  // [t-1][nf] tables of the whole run
+  const float* dft_sin;
+  float *r_pt, *i_pt;  // [nf][nx][ny] accumulators
+  // Set by the launcher: segments that reach a TF/SF edge run as two halves
+  // (their warps carry the slower edge logic).  They are the edge stripes
+  // tf_c[0..nc) with every segment, and the other stripes with the edge
+  // segments tf_r[0..nr); both lists ascending.  nc = nr = 0: no halving.
+  int nc, nr;
+  int tf_c[6], tf_r[6];
+};
+constexpr int kMarchMaxNf = 8;         // DFT frequencies the fused pass carries
+constexpr int kLineMaxNy = 16384;      // incident line held in shared memory
+constexpr int kLineChunkSteps = 64;    // incident-line steps per table
+bool march_ext_supported(const fdtd2d_params& p);
+int launch_march_ext(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out, float* ez, int t0, int k,
+                     int* status, const MarchExt& ext, cudaStream_t st);
+// Advance the incident line (ezinct, hxinct, the input-probe DFT) by nsteps
+// steps t0+1 .. t0+nsteps and record what the 2D update reads of it
+// (fd2d_simple.cu holds the per-step kernels it must equal bit for bit).
+int launch_inc_line(const fdtd2d_params& p, const fdtd2d_state& s, int t0, int nsteps, float* inc_e, float* inc_h,
+                    cudaStream_t st);
+
 }  // namespace fdtd

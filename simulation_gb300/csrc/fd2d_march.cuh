@@ -1,0 +1,660 @@
+// Fused, temporally blocked 2D TM update: the hot kernel of fdtd2d_step_n.
+//
+// This header holds the kernel template; fd2d_march.cu instantiates the
+// plain passes and dispatches, fd2d_march_nf*.cu instantiate the passes with
+// the fd2d_3_4 extras, one translation unit per DFT frequency count.
+//
+// One pass advances the whole grid by K time steps (K = 1..4) while reading
+// every field once from HBM and writing it once: 60 bytes per cell per pass
+// for the lossy PML update (dz, iz, hx, hy, ihx, ihy, naz, nbz in; dz, iz, hx,
+// hy, ihx, ihy, ez out), i.e. 60/K bytes per cell-update.
+//
+// Work decomposition ("streaming march"):
+//   * a warp owns a stripe of 32*CPL columns (CPL = columns per lane, loaded
+//     as one float4/float2), of which the middle 32*CPL-8 are its output and
+//     4 on each side are halo recomputed redundantly;
+//   * the warp walks down a segment of rows.  At row iteration r, level 1
+//     takes input row r, computes D and E on it and completes H on row r-1;
+//     level s takes the row level s-1 just completed (r-s+1) and completes
+//     row r-s at time step s; level K's completed row is stored.  The state a
+//     level carries from one row to the next (the previous row's H, E, D
+//     values) lives in registers, so each cell's K time steps never touch
+//     memory in between;
+//   * the j-neighbours needed by the stencil (hx[j-1] for D, ez[j+1] for H)
+//     come from the adjacent lane by warp shuffle; there is no __syncthreads
+//     and no shared-memory staging of fields at all;
+//   * the i-neighbours come from the row carried in registers.  Segments
+//     overlap by K rows (the dependence cone), so warps are independent.
+// Passes read one copy of the evolving fields and write the other (ping-pong),
+// which makes the overlapping reads race-free.  Out-of-grid lanes/rows load
+// zeros and are masked by the same predicates as the reference loops (no D on
+// row/column 0, no H on the last row/column), so boundary cells see exactly
+// the reference's update.
+//
+// The per-cell arithmetic is the shared inline formulas of fdtd_common.cuh,
+// so a pass of K steps is bitwise identical to K rounds of the per-function
+// kernels (dfield -> source -> efield -> hfield).
+#pragma once
+
+#include <cstdio>
+#include <cstdlib>
+
+#include "fd2d_internal.cuh"
+
+namespace fdtd {
+namespace march {
+
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int HALO = 4;  // halo columns on each side (>= K, multiple of 4 for aligned vectors)
+constexpr int kPlain = -2;        // NFC of the kernels without the fd2d_3_4 extras
+constexpr int kExtMinBlocks = 3;  // blocks per SM the extras kernels are held to
+
+struct MarchArgs {
+  int nx, ny;
+  FieldSet in, out;
+  float* ez;
+  const float* naz;
+  const float* nbz;
+  fdtd2d_pml pml;
+  int src_kind, src_i, src_j;
+  const float* src_table;
+  int t0;
+  int seg_rows, n_stripes, n_segs;
+  int* status;
+  int check_finite;
+  int probe_i, probe_j;  // Ez trace cell (probe_ez != nullptr)
+  float* probe_ez;       // probe_ez[t-1] = ez at the probe after step t
+  MarchExt ext;          // TF/SF corrections and the running DFT (EXT kernels)
+};
+
+// EXT shared memory per warp beyond the PML columns: the DFT ring (lane
+// stride 4*nf floats, made an odd number of 16-byte units) and the twiddles
+// (rounded to 16 bytes)
+__host__ __device__ constexpr int ext_lane_stride(int nf) { return 4 * (nf | 1); }
+__host__ __device__ constexpr int ext_warp_floats(int k, int nf) {
+  return nf > 0 ? k * 32 * ext_lane_stride(nf) + ((2 * nf * k + 3) & ~3) : 0;
+}
+
+struct MarchConfig {
+  int cpl = 0;       // columns per lane; 0 = automatic (measured best: 4 for K <= 2, 2 for K >= 3)
+  int warps = 4;
+  int seg_rows = 0;  // 0 = automatic
+};
+
+extern MarchConfig g_cfg;  // tuning knob (fdtd2d_set_march_config)
+
+// Shortest automatic segment: 4K rows (the recomputed cone is 2K), at least 8.
+// Measured at 1024^2 (adjoint forward/recompute): 8 rows for K <= 2 and 16 for
+// K = 4 beat 16/32 by 1.3-2x, because small grids otherwise leave most SMs idle.
+constexpr int min_seg_rows(int K) { return K * 4 > 8 ? K * 4 : 8; }
+
+// Passes with the extras for one DFT frequency count: nf = 0..4 compiled in,
+// 5..kMarchMaxNf through the runtime-count kernel (fd2d_march_nf*.cu)
+int launch_ext_nf0(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st);
+int launch_ext_nf1(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st);
+int launch_ext_nf2(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st);
+int launch_ext_nf3(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st);
+int launch_ext_nf4(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st);
+int launch_ext_nfrt(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st);
+
+}  // namespace march
+
+namespace {  // kernels are instantiated per translation unit
+
+using namespace march;
+
+template <int CPL>
+__device__ __forceinline__ void ld_row(const float* __restrict__ p, bool ok, float (&v)[CPL]) {
+  if (ok) {
+    if constexpr (CPL == 4) {
+      const float4 x = __ldg(reinterpret_cast<const float4*>(p));
+      v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    } else {
+      const float2 x = __ldg(reinterpret_cast<const float2*>(p));
+      v[0] = x.x; v[1] = x.y;
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) v[c] = 0.f;
+  }
+}
+
+template <int CPL>
+__device__ __forceinline__ void st_row(float* __restrict__ p, const float (&v)[CPL]) {
+  if constexpr (CPL == 4) {
+    __stcs(reinterpret_cast<float4*>(p), make_float4(v[0], v[1], v[2], v[3]));
+  } else {
+    __stcs(reinterpret_cast<float2*>(p), make_float2(v[0], v[1]));
+  }
+}
+
+// global -> shared copy of one lane's accumulator vector, completed by
+// cp_async_wait_all in the same thread (no other thread reads it); a zero
+// fill instead of the read where !ok (src must still be a valid address)
+template <int CPL>
+__device__ __forceinline__ void cp_async_acc_zfill(float* smem_dst, const float* gsrc, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const unsigned n = ok ? 4u * CPL : 0u;
+  if constexpr (CPL == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gsrc), "r"(n) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(gsrc), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+template <int CPL>
+__device__ __forceinline__ bool all_finite(const float (&v)[CPL]) {
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) ok &= isfinite(v[c]);
+  return ok;
+}
+
+// The Ez probe (the adjoint's objective trace) is a separate instantiation,
+// so the benchmark kernels carry no per-cell probe test.  Kernels with
+// 64-column stripes are held to four 4-warp blocks per SM (128 registers, no
+// spills); left free, the compiler takes 138-142 registers and the SM runs
+// three blocks (-9% to -20% at 8192^2, K = 4).  128-column stripes need more
+// registers and are left free.
+//
+// EXT kernels add the fd2d_3_4 extras (fd2d/python/fd2d_3_4.py:90-170) at the
+// same points of each cell's update as the per-step kernels, so they stay
+// bitwise equal to them:
+//   * TF/SF: after D (and the point source), inctdz adds +-hxi/2 on the box's
+//     two j-edges; after H, incthx adds +-ezi/2 to hx on the two j-edges and
+//     incthy +-ezi[j]/2 to hy on the two i-edges.  The incident line is a 1D
+//     problem of its own, advanced ahead of the pass (k_inc_line), so the
+//     pass only reads one table row per time step;
+//   * DFT: each owned cell's accumulators enter a per-warp shared-memory ring
+//     of K rows by cp.async when level 1 reaches the row (one global read),
+//     take one fma per level and frequency there, and leave at level K (one
+//     global write): 16*nf bytes per cell per pass instead of per step, in
+//     the reference's summation order.
+// The level loop is straight-line code that the compiler interleaves across
+// levels; the extras keep it so: edge tests are per-cell selects on uniform
+// table loads, the DFT count is a template constant (NFC = 0..4; NFC = -1
+// reads it at run time) and the ring is updated for every row and lane, with
+// zero-filled copies and predicated stores where the warp does not own the
+// cell.  Branches there cost the EXT kernel 40% at 2048^2.  The edge logic
+// itself is compiled only into the body that warps touching a TF/SF edge run
+// (TF = true: a stripe with an edge column, or rows reaching an edge row);
+// the others run the body without it.
+template <int K, int CPL, bool LOSSY, bool PML, int WARPS, bool PROBE, int NFC, bool TF>
+__device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_x, const int i_s_x, const int i_e_x) {
+  constexpr bool EXT = NFC != kPlain;
+  constexpr bool TFS = EXT && TF;  // this body applies the TF/SF edge corrections
+  constexpr bool DFT = EXT && NFC != 0;  // NFC = -1: count at run time (1..kMarchMaxNf)
+  constexpr int NFMAX = NFC >= 0 ? NFC : kMarchMaxNf;
+  constexpr int W = 32 * CPL;
+  constexpr int OUTW = W - 2 * HALO;
+  static_assert(K >= 1 && K <= HALO, "steps per pass must not exceed the halo");
+  static_assert(!(EXT && PROBE), "the probe trace is not kept by EXT kernels");
+  // per warp: gy2, gy3, fy1, fy2, fy3 of its columns (PML); then (EXT, nf > 0)
+  // the DFT ring [K rows][32 lanes][nf][re0, re1, im0, im1] (lane stride
+  // padded to an odd number of 16-byte units: conflict-free vector access)
+  // and the twiddles [K][nf][cos, -sin]
+  static_assert(!EXT || CPL == 2, "EXT kernels use 64-column stripes");
+  extern __shared__ float smem[];
+
+  const int lane = threadIdx.x & 31;
+  const int wid = threadIdx.x >> 5;
+  // plain kernels map warp -> (stripe, segment) here; EXT kernels get it
+  // from k_march (stripe_x, rows i_s_x .. i_e_x-1)
+  const int gw = blockIdx.x * WARPS + wid;
+  const int stripe = EXT ? stripe_x : gw % a.n_stripes;
+  const int seg = gw / a.n_stripes;
+  if (!EXT && seg >= a.n_segs) return;  // whole warp leaves; nothing below syncs the block
+
+  const int nx = a.nx, ny = a.ny;
+  const int j0 = stripe * OUTW - HALO + lane * CPL;  // first column of this lane (multiple of 4 or 2)
+  const bool vin = (j0 >= 0) && (j0 + CPL <= ny);    // ny % 4 == 0: a vector is wholly in or out
+  const bool vout = vin && (lane * CPL >= HALO) && (lane * CPL < HALO + OUTW);
+
+  const int nf = NFC >= 0 ? NFC : (EXT ? a.ext.nf : 0);
+  const int ls = ext_lane_stride(nf);
+  const int wst = (PML ? 5 * W : 0) + (EXT ? ext_warp_floats(K, nf) : 0);
+  float* const wsm = smem + wid * wst;
+  float* cg = wsm + lane * CPL;
+  float* const ring = wsm + (PML ? 5 * W : 0);
+  float* const tw = ring + K * 32 * ls;
+  if (PML) {
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int j = j0 + c;
+      const bool ok = (j >= 0) && (j < ny);
+      cg[0 * W + c] = ok ? __ldg(a.pml.gy2 + j) : 1.f;
+      cg[1 * W + c] = ok ? __ldg(a.pml.gy3 + j) : 1.f;
+      cg[2 * W + c] = ok ? __ldg(a.pml.fy1 + j) : 0.f;
+      cg[3 * W + c] = ok ? __ldg(a.pml.fy2 + j) : 1.f;
+      cg[4 * W + c] = ok ? __ldg(a.pml.fy3 + j) : 1.f;
+    }
+    __syncwarp();
+  }
+  if constexpr (DFT) {
+    for (int x = lane; x < K * nf; x += 32) {
+      const int s = x / nf, f = x - s * nf;
+      const size_t row = (size_t)(a.t0 + s) * nf + f;  // table row t-1 = t0+s of step t0+s+1
+      tw[2 * x] = __ldg(a.ext.dft_cos + row);
+      tw[2 * x + 1] = -__ldg(a.ext.dft_sin + row);
+    }
+    __syncwarp();
+  }
+  // TF/SF edge columns of this lane: bit 4c+0 D += hxi[np-2]/2, 4c+1 D -=
+  // hxi[ny-np]/2, 4c+2 hx += ezi[np-1]/2, 4c+3 hx -= ezi[ny-np]/2
+  // (TF bodies run only with np > 0: k_march picks them for edge warps)
+  const int np = TFS ? a.ext.tfsf_npml : 0;
+  unsigned tcol = 0;
+  if (TFS && np > 0) {
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int j = j0 + c;
+      if (j == np - 1) tcol |= 1u << (4 * c);
+      if (j == ny - np) tcol |= 2u << (4 * c);
+      if (j == np - 2) tcol |= 4u << (4 * c);
+      if (j == ny - np) tcol |= 8u << (4 * c);
+    }
+  }
+
+  // level state: values of the row each level will complete next
+  float p_hy[K][CPL], p_hx[K][CPL], p_ihx[K][CPL], p_ihy[K][CPL], p_ez[K][CPL], p_dz[K][CPL], p_iz[K][CPL];
+#pragma unroll
+  for (int s = 0; s < K; ++s)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      p_hy[s][c] = p_hx[s][c] = p_ihx[s][c] = p_ihy[s][c] = 0.f;
+      p_ez[s][c] = p_dz[s][c] = p_iz[s][c] = 0.f;
+    }
+
+  const int i_s = EXT ? i_s_x : seg * a.seg_rows;
+  const int i_e = EXT ? i_e_x : min(nx, i_s + a.seg_rows);
+  const int r_begin = max(0, i_s - K);
+  const int r_end = i_e - 1 + K;
+  bool finite_ok = true;
+  const size_t ncell = (size_t)nx * ny;
+  int rk = r_begin % K;  // ring slot of row r (level 1's row); level s uses slot (r - s) mod K
+
+  for (int r = r_begin; r <= r_end; ++r) {
+    // DFT accumulators of row r start their way into the ring now, behind the
+    // field loads (zeros where the warp does not own the cell); level 1 waits
+    // for them after its E update
+    if constexpr (DFT) {
+      const bool own = vout && r >= i_s && r < i_e;
+      const size_t goff = own ? (size_t)r * ny + j0 : 0;
+      float* rg = ring + (rk * 32 + lane) * ls;
+#pragma unroll
+      for (int f = 0; f < NFMAX; ++f) {
+        if (NFC < 0 && f >= nf) break;
+        cp_async_acc_zfill<CPL>(rg + 4 * f, a.ext.r_pt + f * ncell + goff, own);
+        cp_async_acc_zfill<CPL>(rg + 4 * f + 2, a.ext.i_pt + f * ncell + goff, own);
+      }
+      cp_async_commit();
+    }
+    float in_dz[CPL], in_iz[CPL], in_hx[CPL], in_hy[CPL], in_ihx[CPL], in_ihy[CPL];
+    {
+      const bool ok = vin && (r < nx);
+      const size_t off = ok ? (size_t)r * ny + j0 : 0;
+      ld_row<CPL>(a.in.dz + off, ok, in_dz);
+      ld_row<CPL>(a.in.hx + off, ok, in_hx);
+      ld_row<CPL>(a.in.hy + off, ok, in_hy);
+      if (LOSSY) ld_row<CPL>(a.in.iz + off, ok, in_iz);
+      else {
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) in_iz[c] = 0.f;
+      }
+      if (PML) {
+        ld_row<CPL>(a.in.ihx + off, ok, in_ihx);
+        ld_row<CPL>(a.in.ihy + off, ok, in_ihy);
+      } else {
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) in_ihx[c] = in_ihy[c] = 0.f;
+      }
+    }
+
+#pragma unroll
+    for (int s = 0; s < K; ++s) {
+      const int q = r - s;   // row entering level s+1 (time step t0+s+1)
+      const int qc = q - 1;  // row level s+1 completes now
+      const bool qok = (q >= 0) && (q < nx);
+
+      // ---- D (+ point source) and E on row q
+      float naz[CPL], nbz[CPL];
+      {
+        const bool ok = qok && vin;
+        const size_t off = ok ? (size_t)q * ny + j0 : 0;
+        ld_row<CPL>(a.naz + off, ok, naz);
+        if (LOSSY) ld_row<CPL>(a.nbz + off, ok, nbz);
+      }
+      float gx3q = 1.f, gx2q = 1.f;
+      if (PML && qok) {
+        gx3q = __ldg(a.pml.gx3 + q);
+        gx2q = __ldg(a.pml.gx2 + q);
+      }
+      const float hx_left = __shfl_up_sync(FULL, in_hx[CPL - 1], 1);
+      const bool drow = (q >= 1) && (q < nx);
+      bool d_tf = false;  // inctdz row (warp-uniform)
+      float hxi_lo = 0.f, hxi_hi = 0.f;
+      if (TFS) {
+        d_tf = q >= np - 1 && q <= nx - np;
+        hxi_lo = __ldg(a.ext.inc_h + 2 * s);
+        hxi_hi = __ldg(a.ext.inc_h + 2 * s + 1);
+      }
+      float nd[CPL], ne[CPL], niz[CPL];
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const int j = j0 + c;
+        float d = in_dz[c];
+        if (drow && j >= 1 && j < ny) {
+          const float hxm = (c == 0) ? hx_left : in_hx[c - 1];
+          const float gy2 = PML ? cg[0 * W + c] : 1.f;
+          const float gy3 = PML ? cg[1 * W + c] : 1.f;
+          d = d_update(d, in_hy[c], p_hy[s][c], in_hx[c], hxm, gx3q, gy3, gx2q, gy2);
+        }
+        if (a.src_kind != FDTD_SRC_NONE && q == a.src_i && j == a.src_j) {
+          const float v = __ldg(a.src_table + a.t0 + s);
+          d = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(d, v);
+        }
+        if (TFS) {
+          const float d_lo = __fmaf_rn(0.5f, hxi_lo, d), d_hi = __fmaf_rn(-0.5f, hxi_hi, d);
+          d = (d_tf && (tcol & (1u << (4 * c)))) ? d_lo : d;
+          d = (d_tf && (tcol & (2u << (4 * c)))) ? d_hi : d;
+        }
+        float izv = in_iz[c];
+        const float e = LOSSY ? e_update_lossy(d, izv, naz[c], nbz[c]) : e_update(d, naz[c]);
+        nd[c] = d;
+        niz[c] = izv;
+        ne[c] = e;
+        // the probe cell's Ez is recorded by the warp that owns it (output
+        // column, row inside the segment), where every level is valid
+        if (PROBE && q == a.probe_i && j == a.probe_j && vout && q >= i_s && q < i_e) a.probe_ez[a.t0 + s] = e;
+      }
+
+      // ---- running DFT of row q at step t0+s+1 (stored where owned)
+      if constexpr (DFT) {
+        const bool own = vout && q >= i_s && q < i_e;
+        const size_t goff = own ? (size_t)q * ny + j0 : 0;
+        const int slot = rk >= s ? rk - s : rk - s + K;
+        float* rg = ring + (slot * 32 + lane) * ls;
+        const float2* tws = reinterpret_cast<const float2*>(tw) + s * nf;
+        if (s == 0) cp_async_wait_all();
+#pragma unroll
+        for (int f = 0; f < NFMAX; ++f) {
+          if (NFC < 0 && f >= nf) break;
+          float4 v = *reinterpret_cast<const float4*>(rg + 4 * f);  // re0, re1, im0, im1
+          const float2 w = tws[f];                                  // cos, -sin
+          v.x = __fmaf_rn(w.x, ne[0], v.x);
+          v.y = __fmaf_rn(w.x, ne[1], v.y);
+          v.z = __fmaf_rn(w.y, ne[0], v.z);
+          v.w = __fmaf_rn(w.y, ne[1], v.w);
+          if (s == K - 1) {
+            if (own) {
+              __stcs(reinterpret_cast<float2*>(a.ext.r_pt + f * ncell + goff), make_float2(v.x, v.y));
+              __stcs(reinterpret_cast<float2*>(a.ext.i_pt + f * ncell + goff), make_float2(v.z, v.w));
+            }
+          } else {
+            *reinterpret_cast<float4*>(rg + 4 * f) = v;
+          }
+        }
+      }
+
+      // ---- H on row qc (needs Ez of rows qc and q at this level)
+      const float ez_right = __shfl_down_sync(FULL, p_ez[s][0], 1);
+      const bool hrow = (qc >= 0) && (qc <= nx - 2);
+      bool hx_tf = false, hy_tf = false;  // incthx / incthy rows (warp-uniform)
+      float ezi_lo = 0.f, ezi_hi = 0.f, hy_w = 0.f;
+      float ezr[CPL];
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) ezr[c] = 0.f;
+      if (TFS) {
+        const float* erow = a.ext.inc_e + (size_t)s * ny;
+        hx_tf = qc >= np - 1 && qc <= nx - np;
+        ezi_lo = __ldg(erow + max(np - 1, 0));
+        ezi_hi = __ldg(erow + min(ny - np, ny - 1));
+        hy_tf = np > 0 && (qc == np - 2 || qc == nx - np);
+        hy_w = (qc == np - 2) ? -0.5f : 0.5f;
+        ld_row<CPL>(erow + (vin ? j0 : 0), vin && hy_tf, ezr);
+      }
+      float fx1 = 0.f, fx2 = 1.f, fx3 = 1.f;
+      if (PML && hrow) {
+        fx1 = __ldg(a.pml.fx1 + qc);
+        fx2 = __ldg(a.pml.fx2 + qc);
+        fx3 = __ldg(a.pml.fx3 + qc);
+      }
+      float ohx[CPL], ohy[CPL], oihx[CPL], oihy[CPL];
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const int j = j0 + c;
+        float hxv = p_hx[s][c], hyv = p_hy[s][c], ihxv = p_ihx[s][c], ihyv = p_ihy[s][c];
+        if (hrow && j >= 0 && j <= ny - 2) {
+          const float er = (c == CPL - 1) ? ez_right : p_ez[s][c + 1];
+          if (PML)
+            h_update_pml(p_ez[s][c], er, ne[c], hxv, hyv, ihxv, ihyv, fx1, fx2, fx3, cg[2 * W + c], cg[3 * W + c],
+                         cg[4 * W + c]);
+          else
+            h_update_free(p_ez[s][c], er, ne[c], hxv, hyv);
+          if (TFS) {
+            const float x_lo = __fmaf_rn(0.5f, ezi_lo, hxv), x_hi = __fmaf_rn(-0.5f, ezi_hi, hxv);
+            const float y_c = __fmaf_rn(hy_w, ezr[c], hyv);
+            hxv = (hx_tf && (tcol & (4u << (4 * c)))) ? x_lo : hxv;
+            hxv = (hx_tf && (tcol & (8u << (4 * c)))) ? x_hi : hxv;
+            hyv = (hy_tf && j >= np - 1 && j <= ny - np) ? y_c : hyv;
+          }
+        }
+        ohx[c] = hxv;
+        ohy[c] = hyv;
+        oihx[c] = ihxv;
+        oihy[c] = ihyv;
+      }
+
+      // ---- level K stores its completed row
+      if (s == K - 1 && vout && qc >= i_s && qc < i_e) {
+        const size_t off = (size_t)qc * ny + j0;
+        st_row<CPL>(a.out.dz + off, p_dz[s]);
+        st_row<CPL>(a.out.hx + off, ohx);
+        st_row<CPL>(a.out.hy + off, ohy);
+        st_row<CPL>(a.ez + off, p_ez[s]);
+        if (LOSSY) st_row<CPL>(a.out.iz + off, p_iz[s]);
+        if (PML) {
+          st_row<CPL>(a.out.ihx + off, oihx);
+          st_row<CPL>(a.out.ihy + off, oihy);
+        }
+        if (a.check_finite) {
+          finite_ok &= all_finite<CPL>(p_dz[s]) & all_finite<CPL>(ohx) & all_finite<CPL>(ohy) &
+                       all_finite<CPL>(p_ez[s]);
+          if (LOSSY) finite_ok &= all_finite<CPL>(p_iz[s]);
+          if (PML) finite_ok &= all_finite<CPL>(oihx) & all_finite<CPL>(oihy);
+        }
+      }
+
+      // ---- shift: this level's incoming row becomes its "previous" row, and
+      //      the row it completed is the next level's incoming row
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const float t_hy = in_hy[c], t_hx = in_hx[c], t_ihx = in_ihx[c], t_ihy = in_ihy[c];
+        in_dz[c] = p_dz[s][c];
+        in_iz[c] = p_iz[s][c];
+        in_hx[c] = ohx[c];
+        in_hy[c] = ohy[c];
+        in_ihx[c] = oihx[c];
+        in_ihy[c] = oihy[c];
+        p_hy[s][c] = t_hy;
+        p_hx[s][c] = t_hx;
+        p_ihx[s][c] = t_ihx;
+        p_ihy[s][c] = t_ihy;
+        p_ez[s][c] = ne[c];
+        p_dz[s][c] = nd[c];
+        p_iz[s][c] = niz[c];
+      }
+    }
+    rk = (rk + 1 == K) ? 0 : rk + 1;
+  }
+  if (a.check_finite && __any_sync(FULL, !finite_ok) && lane == 0) raise_status(a.status, ST_NONFINITE);
+}
+
+// TF/SF edges a warp's work can reach (np = tfsf_npml > 0): a column np-2,
+// np-1 or ny-np among its stripe's columns (halo included), or a row np-2 or
+// nx-np (hy edges) among the rows its levels update (segment rows widened by
+// the 2K-row cone and the K-row lag).  The launcher builds the halving lists
+// from the same two tests.
+template <int CPL>
+__host__ __device__ inline bool tf_stripe(int np, int ny, int stripe) {
+  constexpr int OUTW = 32 * CPL - 2 * HALO;
+  const int c0 = stripe * OUTW - HALO, c1 = c0 + 32 * CPL - 1;
+  return (np - 2 >= c0 && np - 2 <= c1) || (np - 1 >= c0 && np - 1 <= c1) || (ny - np >= c0 && ny - np <= c1);
+}
+template <int K>
+__host__ __device__ inline bool tf_segment(int np, int nx, int seg_rows, int seg) {
+  const int i_s = seg * seg_rows;
+  const int r0 = i_s - 2 * K, r1 = (i_s + seg_rows < nx ? i_s + seg_rows : nx) + K;
+  return (np - 2 >= r0 && np - 2 <= r1) || (nx - np >= r0 && nx - np <= r1);
+}
+
+__device__ __forceinline__ int pick6(const int (&v)[6], int i) {  // v[i] without a local-memory copy
+  return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : i == 3 ? v[3] : i == 4 ? v[4] : v[5];
+}
+
+// Warp -> work.  Warps 0 .. n_stripes*n_segs-1 take (stripe, segment) as
+// the plain kernels do; with halving on, an edge segment keeps only its first
+// half there and the warps after them take the second halves, first the edge
+// stripes' segments (nc * n_segs), then the edge segments of the other
+// stripes ((n_stripes - nc) * nr).
+template <int K, int CPL, bool LOSSY, bool PML, int WARPS, bool PROBE, int NFC>
+__global__ void __launch_bounds__(WARPS * 32, CPL == 2 ? (NFC == kPlain ? 4 : kExtMinBlocks) : 1)
+    k_march(const MarchArgs a) {
+  const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
+  const int n_base = a.n_stripes * a.n_segs;
+  if constexpr (NFC == kPlain) {
+    march_body<K, CPL, LOSSY, PML, WARPS, PROBE, NFC, false>(a, 0, 0, 0);
+  } else {
+    const int np = a.ext.tfsf_npml;
+    const int nc = a.ext.nc, nr = a.ext.nr;
+    int stripe, seg, half = 0;  // 0: whole segment, 1: first half, 2: second half
+    if (gw < n_base) {
+      stripe = gw % a.n_stripes;
+      seg = gw / a.n_stripes;
+    } else {
+      int k = gw - n_base;
+      if (k < nc * a.n_segs) {
+        stripe = pick6(a.ext.tf_c, k / a.n_segs);
+        seg = k % a.n_segs;
+      } else {
+        k -= nc * a.n_segs;
+        if (k >= (a.n_stripes - nc) * nr) return;
+        seg = pick6(a.ext.tf_r, k % nr);
+        stripe = k / nr;  // the stripe-th stripe not in tf_c (ascending)
+        for (int i = 0; i < nc; ++i)
+          if (pick6(a.ext.tf_c, i) <= stripe) ++stripe;
+      }
+      half = 2;
+    }
+    const bool tf = np > 0 && (tf_stripe<CPL>(np, a.ny, stripe) || tf_segment<K>(np, a.nx, a.seg_rows, seg));
+    if (tf && half == 0 && (nc > 0 || nr > 0)) half = 1;
+    int i_s = seg * a.seg_rows;
+    int i_e = min(a.nx, i_s + a.seg_rows);
+    const int mid = i_s + (i_e - i_s + 1) / 2;
+    if (half == 1) i_e = mid;
+    if (half == 2) i_s = mid;
+    if (i_s >= i_e) return;
+    if (tf)
+      march_body<K, CPL, LOSSY, PML, WARPS, PROBE, NFC, true>(a, stripe, i_s, i_e);
+    else
+      march_body<K, CPL, LOSSY, PML, WARPS, PROBE, NFC, false>(a, stripe, i_s, i_e);
+  }
+}
+
+template <int K, int CPL, bool LOSSY, bool PML, bool PROBE, int NFC = kPlain>
+int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
+  constexpr int WARPS = 4;
+  (void)warps_cfg;
+  MarchArgs a = a0;
+  constexpr int W = 32 * CPL;
+  constexpr int OUTW = W - 2 * HALO;
+  auto kern = k_march<K, CPL, LOSSY, PML, WARPS, PROBE, NFC>;
+  constexpr bool EXT = NFC != kPlain;
+  const int nf = NFC >= 0 ? NFC : (EXT ? a.ext.nf : 0);
+  const size_t smem = (size_t)WARPS * ((PML ? 5 * W : 0) + (EXT ? ext_warp_floats(K, nf) : 0)) * sizeof(float);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      fdtd_host::note_cuda_error(e);
+      return FDTD_ERR_CUDA;
+    }
+  }
+  a.n_stripes = (a.ny + OUTW - 1) / OUTW;
+  int seg_rows = seg_cfg;
+  if (seg_rows <= 0) {
+    int dev = 0, nsm = 0, blocks_per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, WARPS * 32, smem);
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    const long resident = (long)nsm * blocks_per_sm * WARPS;
+    // one wave of warps: n_stripes * n_segs ~= resident warps
+    long n_segs = resident / a.n_stripes;
+    if (EXT && a.ext.tfsf_npml > 0) {
+      // room for the halved edge segments: every segment of the edge
+      // stripes, and about 4 edge segments of the other stripes
+      int nc = 0;
+      for (int q = 0; q < a.n_stripes; ++q) nc += tf_stripe<CPL>(a.ext.tfsf_npml, a.ny, q) ? 1 : 0;
+      n_segs = (resident - 4L * (a.n_stripes - nc)) / (a.n_stripes + nc);
+    }
+    if (n_segs < 1) n_segs = 1;
+    seg_rows = (int)((a.nx + n_segs - 1) / n_segs);
+    // keep the recomputed cone (2K rows per segment) small
+    seg_rows = std::max(seg_rows, min_seg_rows(K));
+  }
+  a.seg_rows = seg_rows;
+  a.n_segs = (a.nx + seg_rows - 1) / seg_rows;
+  long warps = (long)a.n_stripes * a.n_segs;
+  if (EXT) {
+    a.ext.nc = a.ext.nr = 0;
+    const int np = a.ext.tfsf_npml;
+    if (np > 0) {
+      int nc = 0, nr = 0;
+      bool fits = true;
+      for (int q = 0; q < a.n_stripes && fits; ++q)
+        if (tf_stripe<CPL>(np, a.ny, q)) {
+          if (nc == 6) fits = false;
+          else a.ext.tf_c[nc++] = q;
+        }
+      for (int q = 0; q < a.n_segs && fits; ++q)
+        if (tf_segment<K>(np, a.nx, a.seg_rows, q)) {
+          if (nr == 6) fits = false;
+          else a.ext.tf_r[nr++] = q;
+        }
+      if (fits) {  // otherwise edge segments run whole
+        a.ext.nc = nc;
+        a.ext.nr = nr;
+        warps += (long)nc * a.n_segs + (long)(a.n_stripes - nc) * nr;
+      }
+    }
+  }
+  const int blocks = (int)((warps + WARPS - 1) / WARPS);
+  kern<<<blocks, WARPS * 32, smem, st>>>(a);
+  return fdtd_host::check_launch();
+}
+
+template <int NFC, int K>
+int launch_k_ext(const MarchArgs& a, bool lossy, bool pml, cudaStream_t st) {
+  if (lossy && pml) return launch_t<K, 2, true, true, false, NFC>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  if (lossy) return launch_t<K, 2, true, false, false, NFC>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  if (pml) return launch_t<K, 2, false, true, false, NFC>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  return launch_t<K, 2, false, false, false, NFC>(a, g_cfg.warps, g_cfg.seg_rows, st);
+}
+
+// 64-column stripes only: the DFT ring and the edge masks do not fit the
+// 128-column kernel's registers.
+template <int NFC>
+int launch_ext_nfc(const MarchArgs& a, int k, bool lossy, bool pml, cudaStream_t st) {
+  switch (k) {
+    case 1: return launch_k_ext<NFC, 1>(a, lossy, pml, st);
+    case 2: return launch_k_ext<NFC, 2>(a, lossy, pml, st);
+    case 3: return launch_k_ext<NFC, 3>(a, lossy, pml, st);
+    case 4: return launch_k_ext<NFC, 4>(a, lossy, pml, st);
+    default: return FDTD_ERR_ARG;
+  }
+}
+
+}  // namespace
+}  // namespace fdtd

@@ -99,6 +99,72 @@ __global__ void k_ezinct(int ny, float* __restrict__ ezi, const float* __restric
   }
 }
 
+// The incident line advanced nsteps steps in one block, in shared memory,
+// with the same operations as k_ezinct (+ the ABC and the ezi[3] source of
+// k_step_d), the ezi[6] input-probe DFT of k_step_e and k_hxinct, so the
+// line equals the per-step kernels bit for bit.  Per step s it records what
+// the 2D update reads: inc_e[s][:] = ezi after the E update and source, and
+// inc_h[s] = hxi[npml-2], hxi[ny-npml] before the H update.
+__global__ void k_inc_line(int ny, int npml, int t0, int nsteps, float* __restrict__ ezi, float* __restrict__ hxi,
+                           float* __restrict__ bc, const float* __restrict__ tfsf_table, int nf,
+                           const float* __restrict__ dft_cos, const float* __restrict__ dft_sin,
+                           float* __restrict__ r_in, float* __restrict__ i_in, float* __restrict__ inc_e,
+                           float* __restrict__ inc_h) {
+  extern __shared__ float line[];
+  float* e = line;
+  float* h = line + ny;
+  __shared__ float sbc[4];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  for (int j = tid; j < ny; j += nth) {
+    e[j] = ezi[j];
+    h[j] = hxi[j];
+  }
+  if (tid < 4) sbc[tid] = bc[tid];
+  float rin = 0.f, iin = 0.f;
+  if (tid < nf) {
+    rin = r_in[tid];
+    iin = i_in[tid];
+  }
+  __syncthreads();
+  for (int s = 0; s < nsteps; ++s) {
+    const int t = t0 + s + 1;
+    if (tid == 0) {
+      inc_h[2 * s] = h[npml - 2];
+      inc_h[2 * s + 1] = h[ny - npml];
+    }
+    for (int j = 1 + tid; j < ny; j += nth) e[j] = __fmaf_rn(0.5f, __fsub_rn(h[j - 1], h[j]), e[j]);
+    __syncthreads();
+    if (tid == 0) {
+      e[0] = sbc[0];
+      sbc[0] = sbc[1];
+      sbc[1] = e[1];
+      e[ny - 1] = sbc[3];
+      sbc[3] = sbc[2];
+      sbc[2] = e[ny - 2];
+      e[3] = tfsf_table[t - 1];
+    }
+    __syncthreads();
+    float* row = inc_e + (size_t)s * ny;
+    for (int j = tid; j < ny; j += nth) row[j] = e[j];
+    if (tid < nf) {
+      const size_t k = (size_t)(t - 1) * nf + tid;
+      rin = __fmaf_rn(dft_cos[k], e[6], rin);
+      iin = __fmaf_rn(-dft_sin[k], e[6], iin);
+    }
+    for (int j = tid; j < ny - 1; j += nth) h[j] = __fmaf_rn(0.5f, __fsub_rn(e[j], e[j + 1]), h[j]);
+    __syncthreads();
+  }
+  for (int j = tid; j < ny; j += nth) {
+    ezi[j] = e[j];
+    hxi[j] = h[j];
+  }
+  if (tid < 4) bc[tid] = sbc[tid];
+  if (tid < nf) {
+    r_in[tid] = rin;
+    i_in[tid] = iin;
+  }
+}
+
 // inctdz, fd2d/python/fd2d_3_4.py:123-127
 __global__ void k_inctdz(int nx, int ny, int npml, const float* __restrict__ hxi, float* __restrict__ dz) {
   const int i = npml - 1 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -416,6 +482,23 @@ int launch_step3(int t, const fdtd2d_params& p, const fdtd2d_state& s, cudaStrea
   else
     k_step_h<false><<<grid2d(p.nx, p.ny, blk), blk, 0, st>>>(p.nx, p.ny, npml, p.pml, s.ez, nullptr, nullptr, s.hx,
                                                              s.hy, ezi);
+  return fdtd_host::check_launch();
+}
+
+int launch_inc_line(const fdtd2d_params& p, const fdtd2d_state& s, int t0, int nsteps, float* inc_e, float* inc_h,
+                    cudaStream_t st) {
+  const size_t smem = (size_t)2 * p.ny * sizeof(float);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(k_inc_line, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) {
+      fdtd_host::note_cuda_error(e);
+      return FDTD_ERR_CUDA;
+    }
+  }
+  // the input probe is accumulated only with the DFT on (as in fourier)
+  const int nf = p.nf > 0 ? p.nf : 0;
+  k_inc_line<<<1, 1024, smem, st>>>(p.ny, p.tfsf_npml, t0, nsteps, s.ezi, s.hxi, s.bc, p.tfsf_table, nf, p.dft_cos,
+                                    p.dft_sin, s.r_in, s.i_in, inc_e, inc_h);
   return fdtd_host::check_launch();
 }
 

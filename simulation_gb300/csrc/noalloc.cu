@@ -18,7 +18,10 @@
 // path, unchanged.
 //
 // Limits and caveats (also in include/fdtd.h):
-//   * grids whose workspace exceeds the array are rejected with FDTD_ERR_SIZE;
+//   * grids whose workspace exceeds the array are rejected with FDTD_ERR_SIZE,
+//     except with TF/SF or the DFT on, where the incident-line tables may not
+//     fit beside the fields: those runs go one step per fdtd2d_step_n call
+//     (its three-launch form, which needs no workspace);
 //   * the first call on a device resolves the array's address with
 //     cudaGetSymbolAddress; make that first call before any stream capture;
 //   * all calls share the one array and it keeps the last call's contents;
@@ -70,7 +73,14 @@ extern "C" int fdtd2d_step_n_noalloc(const fdtd2d_params* p, fdtd2d_state* s, in
   if (!p || !s) return FDTD_ERR_NULL;
   if ((long long)p->nx * p->ny > (long long)FDTD2D_NOALLOC_MAX_CELLS) return FDTD_ERR_SIZE;
   const size_t need = fdtd2d_workspace_size(p, steps_per_pass);
-  if (need > kScratchBytes) return FDTD_ERR_SIZE;
+  if (need > kScratchBytes) {
+    if (p->tfsf_npml <= 0 && p->nf <= 0) return FDTD_ERR_SIZE;
+    for (int i = 0; i < nsteps; ++i) {
+      const int rc = fdtd2d_step_n(p, s, t0 + i, 1, steps_per_pass, nullptr, 0, stream);
+      if (rc != FDTD_OK) return rc;
+    }
+    return FDTD_OK;
+  }
   void* ws = nullptr;
   if (need > 0) {
     const int rc = scratch_address(&ws);

@@ -39,28 +39,82 @@ def _program_sim(name):
     raise KeyError(name)
 
 
-@pytest.mark.parametrize("nx,ny", [(100, 100), (97, 83)])
-def test_three_launch_step_bitwise_equals_nine_functions(cuda_lib, nx, ny):
-    """With TF/SF, the DFT and a lossy map on, fdtd2d_step_n runs each step as
-    three launches; every field, the incident line, its ABC state and the DFT
-    accumulators equal the nine per-function launches bit for bit."""
+def _extras_sim(nx, ny, lossy, pml, tfsf, nf, ns=256):
     from simulation_gb300 import fd2d as G
+    dt = 0.01 / 6e8
+    naz = nbz = None
+    if lossy:
+        naz, nbz = G.dielectric(nx, ny, 8, 14, dt, 30.0, 0.30)
+    freq = [50e6, 300e6, 700e6, 120e6, 450e6, 900e6, 75e6, 600e6, 222e6][:nf] if nf else None
+    return G.SimTM2D(nx, ny, pml=G.pmlparam(nx, ny, 8) if pml else None, naz=naz, nbz=nbz, lossy=lossy,
+                     tfsf_npml=8 if tfsf else 0, freq=freq, dt=dt, ns=ns,
+                     source=G.PointSource(nx // 3, ny // 3, ("sin", 0.01, 900e6), "soft"))
+
+
+@pytest.mark.parametrize("nx,ny", [(100, 100), (97, 83), (130, 68)])
+@pytest.mark.parametrize("lossy,pml,tfsf,nf", [(True, True, True, 3), (False, True, True, 0), (True, False, True, 1),
+                                               (False, False, False, 8), (True, True, False, 2),
+                                               (True, True, True, 9)])
+def test_extras_bitwise_equal_nine_functions(cuda_lib, nx, ny, lossy, pml, tfsf, nf):
+    """With TF/SF and/or the DFT on, fdtd2d_step_n runs fused passes (the
+    incident line advanced ahead of them in chunks of 64 steps; ny % 4 == 0,
+    nf <= 8) or three launches per step (otherwise); either way every field,
+    the incident line, its ABC state and the DFT accumulators equal the nine
+    per-function launches bit for bit.  150 steps cross a line chunk; the
+    step counts give odd and even pass counts for every steps-per-pass."""
+    for spp, ns in ((4, 150), (3, 70), (1, 5), (2, 9), (0, 131)):
+        a = _extras_sim(nx, ny, lossy, pml, tfsf, nf)
+        b = _extras_sim(nx, ny, lossy, pml, tfsf, nf)
+        a.step(ns, steps_per_pass=spp)
+        b.step_per_function(ns)
+        torch.cuda.synchronize()
+        for k in a.FIELDS:
+            x, y = getattr(a, k), getattr(b, k)
+            if x is None:
+                continue
+            assert torch.equal(x, y), f"spp={spp} ns={ns}: {k} differs (max {float((x - y).abs().max()):.3e})"
+
+
+def test_extras_split_calls_and_graph_replay(cuda_lib):
+    """Calls that start mid-chunk, a one-step call (three launches) between
+    fused calls, and a captured CUDA graph of the fused loop all give the
+    per-function result bit for bit."""
+    a = _extras_sim(128, 128, True, True, True, 3)
+    b = _extras_sim(128, 128, True, True, True, 3)
+    c = _extras_sim(128, 128, True, True, True, 3)
+    for n in (37, 1, 66, 3):
+        a.step(n)
+    b.step_per_function(107)
+    c.run_graph(50)
+    c.run_graph(57)
+    torch.cuda.synchronize()
+    for k in a.FIELDS:
+        if getattr(a, k) is None:
+            continue
+        assert torch.equal(getattr(a, k), getattr(b, k)), f"split calls: {k}"
+        assert torch.equal(getattr(c, k), getattr(b, k)), f"graph: {k}"
+
+
+def test_extras_fd2d_3_4_at_2048(cuda_lib):
+    """The fd2d_3_4 workload of the benchmark (2048^2, PML 32, lossy cylinder,
+    TF/SF, 3-frequency DFT): fused passes equal the per-function launches."""
+    from simulation_gb300 import fd2d as G
+    n = 2048
     dt = 0.01 / 6e8
 
     def make():
-        naz, nbz = G.dielectric(nx, ny, 8, 14, dt, 30.0, 0.30)
-        return G.SimTM2D(nx, ny, pml=G.pmlparam(nx, ny, 8), naz=naz, nbz=nbz, lossy=True, tfsf_npml=8,
-                         freq=[50e6, 300e6, 700e6], dt=dt,
-                         source=G.PointSource(nx // 3, ny // 3, ("sin", 0.01, 900e6), "soft"))
+        naz, nbz = G.dielectric(n, n, 32, n // 8, dt, 30.0, 0.30)
+        return G.SimTM2D(n, n, pml=G.pmlparam(n, n, 32), naz=naz, nbz=nbz, lossy=True, tfsf_npml=32,
+                         freq=[50e6, 300e6, 700e6], dt=dt, ns=200)
     a, b = make(), make()
-    a.step(150)
-    b.step_per_function(150)
+    a.step(90)
+    b.step_per_function(90)
     torch.cuda.synchronize()
     for k in a.FIELDS:
-        x, y = getattr(a, k), getattr(b, k)
-        if x is None:
+        if getattr(a, k) is None:
             continue
-        assert torch.equal(x, y), f"{k} differs"
+        assert torch.equal(getattr(a, k), getattr(b, k)), k
+    assert float(a.r_pt.abs().max()) > 0 and float(a.ez.abs().max()) > 0
 
 
 @pytest.mark.parametrize("name", ["fd2d_3_1", "fd2d_3_2", "fd2d_3_3", "fd2d_3_4"])

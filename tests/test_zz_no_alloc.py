@@ -49,3 +49,29 @@ def test_noalloc_rejects_oversized_grid(cuda_lib):
     s = _lib.State2D()
     p.nx, p.ny = 2048, 1024  # 2^21 cells > FDTD2D_NOALLOC_MAX_CELLS
     assert cuda_lib.fdtd2d_step_n_noalloc(C.byref(p), C.byref(s), 0, 4, 0, None) == -2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [256, 1024])
+def test_noalloc_with_tfsf_and_dft(cuda_lib, n):
+    """TF/SF and a 3-frequency DFT through the allocation-free entry: at 256^2
+    the fused passes (the incident-line tables fit the static array beside the
+    fields), at 1024^2 (the fields alone fill it) one three-launch step per
+    call.  Both equal the per-function launches bit for bit."""
+    from simulation_gb300 import fd2d as G
+    dt = 0.01 / 6e8
+
+    def make():
+        naz, nbz = G.dielectric(n, n, 8, n // 8, dt, 30.0, 0.3)
+        return G.SimTM2D(n, n, pml=G.pmlparam(n, n, 8), naz=naz, nbz=nbz, lossy=True, tfsf_npml=8,
+                         freq=[50e6, 300e6, 700e6], dt=dt, ns=64)
+    a, b = make(), make()
+    st = torch.cuda.current_stream().cuda_stream
+    rc = cuda_lib.fdtd2d_step_n_noalloc(C.byref(a._p), C.byref(a._s), 0, 21, 0, st)
+    assert rc == 0, f"noalloc rc={rc}"
+    b.step_per_function(21)
+    torch.cuda.synchronize()
+    for k in a.FIELDS:
+        if getattr(a, k) is None:
+            continue
+        assert torch.equal(getattr(a, k), getattr(b, k)), f"{n}^2: {k} differs"
