@@ -102,3 +102,34 @@ def test_surrogate_and_gemm_argument_checks_without_gpu(lib):
     g.A, g.B, g.C32 = 0x10000, 0x10000, 0x10000
     g.lda, g.ldb, g.ldc = 65, 64, 128  # 65 BF16 = 130 bytes per row
     assert lib.fdtd_gemm_bf16(C.byref(g), None, None) < 0
+
+
+def test_workspace_size_host_arithmetic(lib):
+    """fdtd2d_workspace_size is host arithmetic: the ping-pong field slots
+    (256-byte rounded), plus 64 incident-line rows of ny floats and 64 (hxi,
+    hxi) pairs with TF/SF on; 0 where the fused pass does not apply."""
+    from simulation_gb300 import _lib
+    lib.fdtd2d_workspace_size.restype = C.c_size_t
+    p = _lib.Params2D()
+    fake = 0x10000
+    p.nx, p.ny = 100, 96
+    slot = (100 * 96 * 4 + 255) // 256 * 256
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 3 * slot  # lossless, no PML
+    p.nbz = fake
+    for k, _ in _lib.Pml2D._fields_:
+        setattr(p.pml, k, fake)
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 6 * slot  # lossy + PML
+    p.nf = 3  # the DFT needs no tables of its own
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 6 * slot
+    p.tfsf_npml = 8
+    line = (64 * 96 * 4 + 255) // 256 * 256 + 512
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 6 * slot + line
+    p.nf = 9  # beyond the fused pass's frequencies: three launches, no workspace
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 0
+    p.nf = 3
+    p.ny = 98  # ny % 4 != 0
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 0
+    p.ny = 16388  # TF/SF line beyond the shared-memory limit
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 0
+    p.tfsf_npml = 0
+    assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 6 * ((100 * 16388 * 4 + 255) // 256 * 256)

@@ -54,6 +54,7 @@ def _extras_sim(nx, ny, lossy, pml, tfsf, nf, ns=256):
 @pytest.mark.parametrize("nx,ny", [(100, 100), (97, 83), (130, 68)])
 @pytest.mark.parametrize("lossy,pml,tfsf,nf", [(True, True, True, 3), (False, True, True, 0), (True, False, True, 1),
                                                (False, False, False, 8), (True, True, False, 2),
+                                               (False, True, True, 4), (True, True, True, 6),
                                                (True, True, True, 9)])
 def test_extras_bitwise_equal_nine_functions(cuda_lib, nx, ny, lossy, pml, tfsf, nf):
     """With TF/SF and/or the DFT on, fdtd2d_step_n runs fused passes (the
