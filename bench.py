@@ -491,12 +491,15 @@ def _bench_surrogate(st, fdtd_spectra_per_s: float | None, n: int = 65536) -> di
 def run_e2e(sim, args, st, world, dev) -> dict:
     """Same runs through SimTM2D with host (pinned) buffers copied in and out.
 
-    Two simulations alternate on two CUDA streams, as a server handling a
-    stream of requests would run them: while one computes, the other's inputs
-    and results cross the host link on the copy engines.  The kernels of the
-    two never overlap (each step's compute waits for the previous step's), so
-    the GPU work per step is that of ``value``; every step still copies all of
-    its inputs in and all of its results out."""
+    Two simulations alternate, as a server handling a stream of requests would
+    run them: while one computes, the other's results and next inputs cross
+    the host link on the copy engines.  Each simulation has an upload, a
+    compute and a download stream; an array's upload waits only for the
+    download of the same array, so the two directions of the link overlap.
+    The kernels of the two simulations never overlap (each step's compute
+    waits for the previous step's), so the GPU work per step is that of
+    ``value``; every step still copies all of its inputs in and all of its
+    results out."""
     import torch
 
     from simulation_gb300 import fd2d as G
@@ -508,24 +511,46 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     pml_host = {k: getattr(sim.pml, k).cpu().pin_memory() for k in sim.pml._fields}
     sims = [sim, G.benchmark_sim(NX, NY, NPML, GRADE, RGRID, EPSR, SIGMA, ns=NS, device=dev,
                                  steps_per_pass=args.spp)]
-    streams = [torch.cuda.Stream(device=dev) for _ in sims]
+    up = [torch.cuda.Stream(device=dev) for _ in sims]
+    comp = [torch.cuda.Stream(device=dev) for _ in sims]
+    down = [torch.cuda.Stream(device=dev) for _ in sims]
     host_out = [{k: torch.empty((NX, NY), dtype=torch.float32, pin_memory=True) for k in keys_out} for _ in sims]
+    out_done = [{} for _ in sims]  # array -> event: its last download finished reading the device buffer
+    last_compute = [None for _ in sims]  # this simulation's previous compute (it reads every input)
+    # inputs that are not downloaded go first, while the other arrays are still on their way out
+    order_in = [k for k in keys_in if k not in keys_out] + [k for k in keys_in if k in keys_out]
 
     def one(k, prev_done):
-        s, o, x = sims[k % 2], host_out[k % 2], streams[k % 2]
-        with torch.cuda.stream(x):
-            for key in keys_in:
+        i = k % 2
+        s, o = sims[i], host_out[i]
+        with torch.cuda.stream(up[i]):
+            if last_compute[i] is not None:
+                up[i].wait_event(last_compute[i])
+            for key in order_in:
+                ev = out_done[i].get(key)
+                if ev is not None:
+                    up[i].wait_event(ev)
                 getattr(s, key).copy_(host_in[key], non_blocking=True)
             for key, v in pml_host.items():
                 getattr(s.pml, key).copy_(v, non_blocking=True)
+            inputs = torch.cuda.Event()
+            inputs.record(up[i])
+        with torch.cuda.stream(comp[i]):
+            comp[i].wait_event(inputs)
             if prev_done is not None:
-                x.wait_event(prev_done)  # compute after the previous step's compute
+                comp[i].wait_event(prev_done)  # compute after the previous step's compute
             s.t = 0
             s.step(NS)
             done = torch.cuda.Event()
-            done.record(x)
+            done.record(comp[i])
+            last_compute[i] = done
+        with torch.cuda.stream(down[i]):
+            down[i].wait_event(done)
             for key in keys_out:
                 o[key].copy_(getattr(s, key), non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(down[i])
+                out_done[i][key] = ev
         return done
 
     done = None
@@ -534,12 +559,12 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
-    for x in streams:
+    for x in up + comp + down:
         x.wait_stream(st)
     done = None
     for k in range(args.steps):
         done = one(k, done)
-    for x in streams:
+    for x in up + comp + down:
         st.wait_stream(x)
     e1.record(st)
     torch.cuda.synchronize()
@@ -551,7 +576,7 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     del sims[1]
     return {"value": NX * NY * NS * args.steps * world / (ms / 1e3) / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms / args.steps,
-            "simulations_in_flight": 2}
+            "simulations_in_flight": 2, "copy_streams": "upload and download per simulation"}
 
 
 def main():
