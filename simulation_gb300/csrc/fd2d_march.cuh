@@ -74,7 +74,7 @@ struct MarchArgs {
   MarchExt ext;          // TF/SF corrections and the running DFT (EXT kernels)
 };
 
-// EXT shared memory per warp beyond the PML columns, in floats (each part a
+// Shared memory per warp beyond the PML columns, in floats (each part a
 // multiple of 4): the DFT ring (K+1 rows; lane stride 4*nf floats made an odd
 // number of 16-byte units, so 16-byte accesses are conflict-free), the
 // twiddles, the field-row ring (2 rows of the 3-6 evolving fields) and the
@@ -177,27 +177,7 @@ __device__ __forceinline__ bool all_finite(const float (&v)[CPL]) {
   return ok;
 }
 
-// The Ez probe (the adjoint's objective trace) is a separate instantiation,
-// so the benchmark kernels carry no per-cell probe test.  Kernels with
-// 64-column stripes are held to four 4-warp blocks per SM (128 registers, no
-// spills); left free, the compiler takes 138-142 registers and the SM runs
-// three blocks (-9% to -20% at 8192^2, K = 4).  128-column stripes need more
-// registers and are left free.
-//
-// EXT kernels add the fd2d_3_4 extras (fd2d/python/fd2d_3_4.py:90-170) at the
-// same points of each cell's update as the per-step kernels, so they stay
-// bitwise equal to them:
-//   * TF/SF: after D (and the point source), inctdz adds +-hxi/2 on the box's
-//     two j-edges; after H, incthx adds +-ezi/2 to hx on the two j-edges and
-//     incthy +-ezi[j]/2 to hy on the two i-edges.  The incident line is a 1D
-//     problem of its own, advanced ahead of the pass (k_inc_line), so the
-//     pass only reads one table row per time step;
-//   * DFT: each owned cell's accumulators enter a per-warp shared-memory ring
-//     of K rows by cp.async when level 1 reaches the row (one global read),
-//     take one fma per level and frequency there, and leave at level K (one
-//     global write): 16*nf bytes per cell per pass instead of per step, in
-//     the reference's summation order.
-// EXT prefetch of one row by cp.async (zero fill outside the grid, as ld_row
+// Prefetch of one row by cp.async (zero fill outside the grid, as ld_row
 // does): the evolving fields into a field-ring slot `fr` ([NFA][W], this
 // lane's columns), naz/nbz into a material-ring slot `mr`, the DFT
 // accumulators of owned cells into a DFT-ring slot `rg`
@@ -235,6 +215,27 @@ __device__ __forceinline__ void pf_dft(const MarchArgs& a, float* rg, int row, i
   }
 }
 
+// The Ez probe (the adjoint's objective trace) is a separate instantiation,
+// so the benchmark kernels carry no per-cell probe test.  Plain kernels with
+// 64-column stripes are held to four 4-warp blocks per SM (128 registers; the
+// K = 4 lossy PML one spills 8 bytes since the row prefetch); left free, the
+// compiler takes 138-142 registers and the SM runs three blocks (-9% to -20%
+// at 8192^2, K = 4).  128-column stripes need more registers and are left
+// free.  The EXT kernels need about 160 and are held to three blocks.
+//
+// EXT kernels add the fd2d_3_4 extras (fd2d/python/fd2d_3_4.py:90-170) at the
+// same points of each cell's update as the per-step kernels, so they stay
+// bitwise equal to them:
+//   * TF/SF: after D (and the point source), inctdz adds +-hxi/2 on the box's
+//     two j-edges; after H, incthx adds +-ezi/2 to hx on the two j-edges and
+//     incthy +-ezi[j]/2 to hy on the two i-edges.  The incident line is a 1D
+//     problem of its own, advanced ahead of the pass (k_inc_line), so the
+//     pass only reads one table row per time step;
+//   * DFT: each owned cell's accumulators enter a per-warp shared-memory ring
+//     of K+1 rows by cp.async with the row's fields (one global read), take
+//     one fma per level and frequency there, and leave at level K (one
+//     global write): 16*nf bytes per cell per pass instead of per step, in
+//     the reference's summation order.
 // The level loop is straight-line code that the compiler interleaves across
 // levels; the extras keep it so: edge tests are per-cell selects on uniform
 // table loads, the DFT count is a template constant (NFC = 0..4; NFC = -1
@@ -255,10 +256,11 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
   constexpr int OUTW = W - 2 * HALO;
   static_assert(K >= 1 && K <= HALO, "steps per pass must not exceed the halo");
   static_assert(!(EXT && PROBE), "the probe trace is not kept by EXT kernels");
-  // per warp: gy2, gy3, fy1, fy2, fy3 of its columns (PML); then (EXT, nf > 0)
-  // the DFT ring [K rows][32 lanes][nf][re0, re1, im0, im1] (lane stride
+  // per warp: gy2, gy3, fy1, fy2, fy3 of its columns (PML); then (nf > 0)
+  // the DFT ring [K+1 rows][32 lanes][nf][re0, re1, im0, im1] (lane stride
   // padded to an odd number of 16-byte units: conflict-free vector access)
-  // and the twiddles [K][nf][cos, -sin]
+  // and the twiddles [K][nf][cos, -sin]; then the field-row ring [2][NFA][W]
+  // and the material-row ring [K+1][NMA][W]
   static_assert(!EXT || CPL == 2, "EXT kernels use 64-column stripes");
   extern __shared__ float smem[];
 
@@ -277,7 +279,7 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
   const bool vout = vin && (lane * CPL >= HALO) && (lane * CPL < HALO + OUTW);
 
   const int nf = NFC >= 0 ? NFC : (EXT ? a.ext.nf : 0);
-  // EXT: rows are prefetched one iteration ahead by cp.async; M rows of the
+  // rows are prefetched one iteration ahead by cp.async; M rows of the
   // DFT and material rings are in use at once (levels 1..K and the next row)
   constexpr int M = K + 1;
   constexpr int NFA = ext_nfields(LOSSY, PML);  // fields in the row ring: dz, hx, hy, [iz], [ihx, ihy]
