@@ -168,6 +168,23 @@ def cpu_port_rate(nx: int, ny: int, steps: int, threads: int | None = None) -> d
             "sample": f"{nx}x{ny} grid, {steps} steps of the same lossy PML update (float32 C port, OpenMP)"}
 
 
+def numpy_reference_rate(n: int = 2048, steps: int = 10) -> dict:
+    """Time the reference's own NumPy form of the step (the oracle's float64
+    restatement of fd2d/program/fd2d_3_2.py:61-93 with the lossy efield of
+    fd2d/python/fd2d_3_4.py:131-136) on a bounded sample, one host thread."""
+    from oracle import fd2d as O
+    dt = 0.01 / 6e8
+    pml = O.pmlparam(n, n, NPML, GRADE)
+    naz, nbz = O.dielectric(n, n, NPML, n // 8, dt, EPSR, SIGMA)
+    src = ("hard", n // 2, n // 2, ("gauss", 20, 6.0))
+    st = O.run(n, n, 1, pml=pml, naz=naz, nbz=nbz, src=src)  # warm-up step
+    t0 = time.perf_counter()
+    O.run(n, n, steps, pml=pml, naz=naz, nbz=nbz, src=src, state=st, t_start=2)
+    el = time.perf_counter() - t0
+    return {"value": n * n * steps / el / 1e9, "seconds": el, "cores": 1,
+            "sample": f"{n}x{n} grid, {steps} steps of the float64 NumPy form of the reference step"}
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -280,6 +297,10 @@ def run_ours(args) -> None:
         cpu["kind"] = "port"
         one = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS_1T", "10")), threads=1)
         cpu["single_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
+        try:
+            cpu["numpy_reference_form"] = numpy_reference_rate()
+        except Exception as exc:  # reported, never fatal to the bench line
+            cpu["numpy_reference_form"] = {"error": f"{type(exc).__name__}: {exc}"}
         from oracle import ccore
         ccore.lib32().oracle_set_threads(cpu["cores"])
 
