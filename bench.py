@@ -398,7 +398,19 @@ def _bench_fd1d(st, reps: int = 20) -> dict:
     e1.record(st)
     torch.cuda.synchronize()
     us = e0.elapsed_time(e1) * 1e3 / reps
-    return {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3, "kernel_launches_per_run": 1}
+    res = {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3, "kernel_launches_per_run": 1}
+    try:  # the same run through the reference's NumPy form (float64 restatement), one host thread
+        from oracle import fd1d as O1
+        kw = O1.program("config1")
+        O1.run(**kw)
+        t0 = time.perf_counter()
+        O1.run(**kw)
+        el = time.perf_counter() - t0
+        res["cpu_baseline"] = {"us_per_run": el * 1e6, "cores": 1, "kind": "port",
+                               "sample": "one config-1 run (ke=200, 1000 steps), float64 NumPy form of the reference"}
+    except Exception as exc:  # reported, never fatal to the bench line
+        res["cpu_baseline"] = {"error": f"{type(exc).__name__}: {exc}"}
+    return res
 
 
 def _bench_batch1d(st, nruns: int = 4096, autotune: bool = True, cpu: bool = False) -> dict:
