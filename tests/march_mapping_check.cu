@@ -12,7 +12,8 @@
 //     that a TF/SF correction applies to (an edge column in its stripe, halo
 //     included, or an hy edge row among the rows its levels complete).
 // The list building and the warp enumeration below restate launch_t and
-// k_march's extras branch line for line.
+// k_march's extras branch line for line.  It also checks that every
+// instantiation's dynamic shared memory fits a block.
 #include <algorithm>
 #include <cstdio>
 #include <vector>
@@ -120,9 +121,28 @@ void sweep() {
       }
 }
 
+// Dynamic shared memory of every instantiation (launch_t's formula) fits the
+// 227 KB a block may have: 64- and 128-column stripes, K = 1..4, 0..8 DFT
+// frequencies (the extras use 64-column stripes only).
+void check_shared_memory() {
+  constexpr int kWarps = 4;
+  for (int cpl : {2, 4})
+    for (int k = 1; k <= 4; ++k)
+      for (int nf = 0; nf <= fdtd::kMarchMaxNf; ++nf)
+        for (int lossy = 0; lossy < 2; ++lossy)
+          for (int pml = 0; pml < 2; ++pml) {
+            if (cpl == 4 && nf > 0) continue;
+            const int w = 32 * cpl;
+            const long bytes = (long)kWarps * ((pml ? 5 * w : 0) +
+                                               fdtd::march::ext_warp_floats(k, nf, lossy, pml, w)) * 4;
+            if (bytes > 227L * 1024) fail("shared memory over 227 KB", cpl, k, nf, lossy, pml, (int)bytes, 0);
+          }
+}
+
 }  // namespace
 
 int main() {
+  check_shared_memory();
   sweep<1>();
   sweep<2>();
   sweep<3>();
