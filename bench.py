@@ -168,6 +168,22 @@ def cpu_port_rate(nx: int, ny: int, steps: int, threads: int | None = None) -> d
             "sample": f"{nx}x{ny} grid, {steps} steps of the same lossy PML update (float32 C port, OpenMP)"}
 
 
+def max_over_ranks(ms: float, world: int, device) -> float:
+    """The slowest rank's time: replicas finish when the last one does."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(cell_updates_per_rank: int, world: int, ms: float) -> float:
+    """Gcell-updates/s of the whole job: every rank's work over the slowest time."""
+    return cell_updates_per_rank * world / (ms / 1e3) / 1e9
+
+
 def numpy_reference_rate(n: int = 2048, steps: int = 10) -> dict:
     """Time the reference's own NumPy form of the step (the oracle's float64
     restatement of fd2d/program/fd2d_3_2.py:61-93 with the lossy efield of
@@ -257,12 +273,8 @@ def run_ours(args) -> None:
     clocks = clk.stop()
     ms = e0.elapsed_time(e1)
     sim.check()
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    total_cells = cells * NS * args.steps * world
-    value = total_cells / (ms / 1e3) / 1e9
+    ms = max_over_ranks(ms, world, dev)
+    value = whole_job_rate(cells * NS * args.steps, world, ms)
 
     # dominant kernel: time fused passes individually (2 passes of spp steps)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(10)]
@@ -611,7 +623,8 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     h2d = sum(v.numel() * 4 for v in host_in.values()) + sum(v.numel() * 4 for v in pml_host.values())
     d2h = sum(v.numel() * 4 for v in host_out[0].values())
     del sims[1]
-    return {"value": NX * NY * NS * steps * world / (ms / 1e3) / 1e9, "unit": UNIT,
+    ms = max_over_ranks(ms, world, dev)
+    return {"value": whole_job_rate(NX * NY * NS * steps, world, ms), "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms / steps, "steps": steps,
             "simulations_in_flight": 2, "copy_streams": "upload and download per simulation"}
 
