@@ -117,6 +117,12 @@ typedef struct {
    * probe_ez[t-1] = ez[probe_i][probe_j] after step t; probe_len entries */
   int probe_i, probe_j;
   int probe_len;
+  /* thickness of the absorbing layer in cells (npml of the reference's
+   * programs, e.g. fd2d/python/fd2d_3_2.py:133), or 0 if not given.  A hint
+   * for laying out the fused kernel's work only: which cells run the cheaper
+   * interior update is decided on the device from the PML vectors
+   * themselves, so results never depend on it. */
+  int pml_cells;
 } fdtd2d_params;
 
 typedef struct {
@@ -176,6 +182,12 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
  * wave of warps).
  * No reference counterpart. */
 int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows);
+/* Tuning knob of the fused kernel's work layout: the time of a general row
+ * iteration (PML coefficients, grid edges, source) over an interior one,
+ * used to give the stripes and segments that hold the absorbing layer
+ * shorter work (1..16; 0 = the measured default for the stripe width).
+ * No reference counterpart. */
+int fdtd2d_set_march_balance(float gen_cost);
 
 /* fdtd2d_step_n without a caller-provided workspace, for callers that cannot
  * allocate device memory (no cudaMalloc available or allowed where they run).
@@ -220,6 +232,45 @@ int fdtd2d_pass(const fdtd2d_params* p, const fdtd2d_fields* in, fdtd2d_fields* 
 int fdtd2d_adjoint_step(int t, const fdtd2d_params* p, const fdtd2d_fields* fwd, fdtd2d_fields* adj, float* adj_tmp,
                         int probe_i, int probe_j, float probe_weight, fdtd2d_box box, float* grad_naz,
                         float* grad_nbz, fdtd_stream_t stream);
+
+/* The whole gradient in one call.  J = sum over t = 1..nsteps of
+ * (probe_weight/2) * ez_t[probe_i][probe_j]^2 for the program `p` run from
+ * zero fields (PML required: pass unit profiles for none; point source only;
+ * ny % 4 == 0); grad_naz [box.ni][box.nj] receives dJ/dnaz over the box and
+ * grad_nbz (optional, lossy only) dJ/dnbz (dJ/deps_r = -naz^2 dJ/dnaz for
+ * naz = 1/(eps_r + sigma*dt/eps0)).
+ *   forward: fused passes with a stored state every `checkpoint` steps; the
+ *            probe's Ez goes to trace [nsteps] (device) and J (device double,
+ *            optional) is summed from it;
+ *   reverse: segments last first, each recomputed from its checkpoint by
+ *            passes that record the state after every step (on a second,
+ *            internal stream, one segment ahead), then undone one step per
+ *            fused reverse kernel.
+ * fdtd2d_tm_adjoint runs both; _forward and _reverse run one each, sharing
+ * the workspace (the reverse needs the forward's checkpoints).  The workspace
+ * (fdtd2d_tm_adjoint_workspace_size bytes, 256-byte aligned) holds the
+ * checkpoints, two segments of recorded states and the ping-pong fields.  The
+ * first call on a device creates the internal stream and its events: make it
+ * before any stream capture; later calls can be captured.  The gradient does
+ * not depend on the checkpoint interval.
+ * Replaces the time loop of fd2d/python/fd2d_3_2.py:139-142 (forward) and
+ * adds its reverse, which the reference does not have. */
+typedef struct {
+  int nsteps;
+  int checkpoint;
+  int probe_i, probe_j;
+  float probe_weight;
+  fdtd2d_box box;
+} fdtd2d_adjoint_params;
+
+size_t fdtd2d_tm_adjoint_workspace_size(const fdtd2d_params* p, const fdtd2d_adjoint_params* a);
+int fdtd2d_tm_adjoint_forward(const fdtd2d_params* p, const fdtd2d_adjoint_params* a, float* trace, double* J,
+                              void* workspace, size_t workspace_bytes, fdtd_stream_t stream);
+int fdtd2d_tm_adjoint_reverse(const fdtd2d_params* p, const fdtd2d_adjoint_params* a, float* grad_naz,
+                              float* grad_nbz, void* workspace, size_t workspace_bytes, fdtd_stream_t stream);
+int fdtd2d_tm_adjoint(const fdtd2d_params* p, const fdtd2d_adjoint_params* a, float* trace, double* J,
+                      float* grad_naz, float* grad_nbz, void* workspace, size_t workspace_bytes,
+                      fdtd_stream_t stream);
 
 /* ------------------------------------------------ BF16 tensor-core GEMM
  * D = epilogue(alpha * A.B) on sm_103a tensor cores (tcgen05, TMA, TMEM),
@@ -316,6 +367,17 @@ int fno_to_bf16(long long n, const float* x, void* y, fdtd_stream_t stream);
  * writes naz, nbz [nx][ny]. */
 int fdtd2d_dielectric_cylinder(int nx, int ny, int npml, double rgrid, double dt, double epsr,
                                double sigma, float* naz, float* nbz, fdtd_stream_t stream);
+
+/* Amplitude and phase of running-DFT accumulators against the input probe,
+ * in double: amp = 1/hypot(r_in, i_in) * hypot(r_pt, i_pt) and phase =
+ * atan2(i_pt, r_pt) - atan2(i_in, r_in), for f < nf and k < n, where the
+ * accumulators of frequency f are r_pt[f*ld + k] (so a 2D row is r_pt +
+ * row*ny with ld = nx*ny) and the input's are r_in[f]; amp/phase [nf][n]
+ * (either may be NULL).  Replaces the post-processing of
+ * fd1d/program/fd1d_2_2.py:145-146 and fd2d/python/fd2d_3_4.py:280-284. */
+int fdtd_dft_amplitude_phase(int nf, long long n, const float* r_pt, const float* i_pt, long long ld,
+                             const float* r_in, const float* i_in, double* amp, double* phase,
+                             fdtd_stream_t stream);
 
 /* Sets *status_out |= FDTD_STATUS_NONFINITE if any of the n floats is Inf/NaN. */
 int fdtd_check_finite(const float* x, size_t n, int* status, fdtd_stream_t stream);

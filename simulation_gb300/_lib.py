@@ -56,7 +56,7 @@ class Params2D(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("pml", Pml2D), ("naz", F), ("nbz", F), ("src", Source2D),
                 ("tfsf_npml", C.c_int), ("tfsf_table", F), ("tfsf_table_len", C.c_int),
                 ("nf", C.c_int), ("dft_cos", F), ("dft_sin", F), ("dft_table_len", C.c_int),
-                ("probe_i", C.c_int), ("probe_j", C.c_int), ("probe_len", C.c_int)]
+                ("probe_i", C.c_int), ("probe_j", C.c_int), ("probe_len", C.c_int), ("pml_cells", C.c_int)]
 
 
 class State2D(C.Structure):
@@ -70,6 +70,11 @@ class Fields2D(C.Structure):
 
 class Box2D(C.Structure):
     _fields_ = [("i0", C.c_int), ("j0", C.c_int), ("ni", C.c_int), ("nj", C.c_int)]
+
+
+class AdjointParams2D(C.Structure):
+    _fields_ = [("nsteps", C.c_int), ("checkpoint", C.c_int), ("probe_i", C.c_int), ("probe_j", C.c_int),
+                ("probe_weight", C.c_float), ("box", Box2D)]
 
 
 class GemmDesc(C.Structure):
@@ -124,10 +129,18 @@ _SIGS = {
     "fdtd2d_step_n": ([C.POINTER(Params2D), C.POINTER(State2D), C.c_int, C.c_int, C.c_int, P, C.c_size_t, P],
                       C.c_int),
     "fdtd2d_set_march_config": ([C.c_int, C.c_int, C.c_int], C.c_int),
+    "fdtd2d_set_march_balance": ([C.c_float], C.c_int),
     "fdtd2d_pass": ([C.POINTER(Params2D), C.POINTER(Fields2D), C.POINTER(Fields2D), F, C.c_int, C.c_int, P, P],
                     C.c_int),
     "fdtd2d_adjoint_step": ([C.c_int, C.POINTER(Params2D), C.POINTER(Fields2D), C.POINTER(Fields2D), F, C.c_int,
                              C.c_int, C.c_float, Box2D, F, F, P], C.c_int),
+    "fdtd2d_tm_adjoint_workspace_size": ([C.POINTER(Params2D), C.POINTER(AdjointParams2D)], C.c_size_t),
+    "fdtd2d_tm_adjoint_forward": ([C.POINTER(Params2D), C.POINTER(AdjointParams2D), F, P, P, C.c_size_t, P],
+                                  C.c_int),
+    "fdtd2d_tm_adjoint_reverse": ([C.POINTER(Params2D), C.POINTER(AdjointParams2D), F, F, P, C.c_size_t, P],
+                                  C.c_int),
+    "fdtd2d_tm_adjoint": ([C.POINTER(Params2D), C.POINTER(AdjointParams2D), F, P, F, F, P, C.c_size_t, P], C.c_int),
+    "fdtd_dft_amplitude_phase": ([C.c_int, C.c_longlong, F, F, C.c_longlong, F, F, P, P, P], C.c_int),
     "fdtd2d_step_n_noalloc": ([C.POINTER(Params2D), C.POINTER(State2D), C.c_int, C.c_int, C.c_int, P], C.c_int),
     "fdtd2d_dielectric_cylinder": ([C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                     F, F, P], C.c_int),

@@ -6,14 +6,15 @@ The forward map is the lossy 2D TM update with PML of the reference
 with a Gaussian point source; the objective is J = sum_t Ez_t(probe)^2.  The
 reference has no derivative; this is the library's extension.
 
-Forward: the fused kernel (``fdtd2d_step_n``) runs the time loop, records
-Ez at the probe every step and copies the fields to a checkpoint every
-``checkpoint`` steps.  Reverse: for each segment, last first, the states of
-the segment are recomputed from its checkpoint (``fdtd2d_pass``, one step per
-pass, bitwise equal to the forward; on a second stream, one segment ahead of
-the sweep), then ``fdtd2d_adjoint_step`` walks the segment backwards
-accumulating dJ/dnaz on the design box;
-dJ/deps_r = -naz^2 * dJ/dnaz since naz = 1/(eps_r + sigma*dt/eps0).
+The whole schedule is one C-ABI call each way (``fdtd2d_tm_adjoint_forward``
+and ``fdtd2d_tm_adjoint_reverse``, or both in ``fdtd2d_tm_adjoint``): the
+forward runs fused passes with a stored state every ``checkpoint`` steps and
+records Ez at the probe; the reverse recomputes each segment from its
+checkpoint with passes that record every step's state (on a second stream,
+one segment ahead) and undoes the steps with one fused reverse kernel each,
+accumulating dJ/dnaz on the design box.  dJ/deps_r = -naz^2 * dJ/dnaz since
+naz = 1/(eps_r + sigma*dt/eps0).  This module only holds the tensors and the
+workspace and calls the library.
 
 ``FdtdObjective`` wraps forward + reverse as a torch.autograd.Function.
 """
@@ -60,16 +61,15 @@ class AdjointProblem:
                            source=PointSource(self.src[0], self.src[1], wave, src_kind), ns=ns, device=device,
                            check_finite=True)
         self.trace = torch.zeros(ns, dtype=torch.float32, device=self.device)
-        self.sim._p.probe_i, self.sim._p.probe_j, self.sim._p.probe_len = self.probe[0], self.probe[1], ns
-        self.sim._s.probe_ez = self.trace.data_ptr()
+        self.J_dev = torch.zeros(1, dtype=torch.float64, device=self.device)
+        self.grad_naz = torch.zeros((bi, bj), dtype=torch.float32, device=self.device)
         self.ncp = -(-ns // checkpoint)
-        z = lambda *s: torch.zeros(s, dtype=torch.float32, device=self.device)  # noqa: E731
-        self.ckpt = z(self.ncp, 6, nx, ny)
-        self.seg = z(2, checkpoint, 6, nx, ny)  # two segments: one recomputed while the other is swept
-        self.adj = z(6, nx, ny)
-        self.tmp = z(nx, ny)
-        self.ez_scratch = z(nx, ny)
-        self.grad_naz = z(bi, bj)
+        self.ap = _lib.AdjointParams2D(ns, checkpoint, self.probe[0], self.probe[1], 2.0,
+                                       _lib.Box2D(*self.box))
+        n = _lib.lib().fdtd2d_tm_adjoint_workspace_size(C.byref(self.sim._p), C.byref(self.ap))
+        if n == 0:
+            raise ValueError("fdtd2d_tm_adjoint_workspace_size rejected the problem")
+        self.ws = torch.empty(n, dtype=torch.uint8, device=self.device)
         self.J = None
         # the loops are static for a problem (pointers, steps, segment order):
         # from the second call on, each sweep replays a CUDA graph of itself
@@ -87,14 +87,6 @@ class AdjointProblem:
         self.sim.nbz.zero_()
         self.sim.naz[i0:i0 + bi, j0:j0 + bj] = (1.0 / (e + nb)).float()
         self.sim.nbz[i0:i0 + bi, j0:j0 + bj] = nb
-
-    FIELDS = ("dz", "iz", "hx", "hy", "ihx", "ihy")
-
-    def _fields(self, buf) -> _lib.Fields2D:
-        f = _lib.Fields2D()
-        for k, name in enumerate(self.FIELDS):
-            setattr(f, name, buf[k].data_ptr())
-        return f
 
     # ------------------------------------------------------------ forward
     def _run(self, name: str, body) -> None:
@@ -118,82 +110,25 @@ class AdjointProblem:
 
     def forward(self) -> float:
         """Run the time loop with checkpoints; returns J = sum_t Ez_t(probe)^2."""
-        s = self.sim
-
         def body():
-            s.reset()
-            self.trace.zero_()
-            for c in range(self.ncp):
-                for k, name in enumerate(self.FIELDS):
-                    self.ckpt[c, k].copy_(getattr(s, name))
-                s.step(min(self.cp, self.ns - c * self.cp))
+            _lib.call("fdtd2d_tm_adjoint_forward", C.byref(self.sim._p), C.byref(self.ap), self.trace.data_ptr(),
+                      self.J_dev.data_ptr(), self.ws.data_ptr(), self.ws.numel(), _lib.stream_ptr())
 
         self._run("forward", body)
-        s.t = self.ns
-        self.J = float((self.trace.double() ** 2).sum())
+        self.sim.t = self.ns
+        self.J = float(self.J_dev.item())
         return self.J
 
     # ------------------------------------------------------------ reverse
     def gradient_naz(self) -> torch.Tensor:
-        """dJ/dnaz on the design box (float32 [bi][bj]) by the reverse sweep.
+        """dJ/dnaz on the design box (float32 [bi][bj]) by the reverse sweep
+        over the checkpoints of the last ``forward``."""
+        def body():
+            _lib.call("fdtd2d_tm_adjoint_reverse", C.byref(self.sim._p), C.byref(self.ap),
+                      self.grad_naz.data_ptr(), None, self.ws.data_ptr(), self.ws.numel(), _lib.stream_ptr())
 
-        Segments are swept last first.  While the current stream walks segment
-        c backwards, a second stream recomputes the states of segment c-1 into
-        the other half of ``seg``; events order each buffer's reuse.  The work
-        per kernel is unchanged, so the gradient is the same bit for bit."""
-        if not hasattr(self, "_side"):
-            self._side = torch.cuda.Stream(device=self.device)
-        self._run("reverse", self._reverse)
+        self._run("reverse", body)
         return self.grad_naz
-
-    def _reverse(self) -> None:
-        lib = _lib.lib()
-        main = torch.cuda.current_stream(self.device)
-        side = self._side
-        st_main, st_side = main.cuda_stream, side.cuda_stream
-        p = self.sim._p
-        self.adj.zero_()
-        self.grad_naz.zero_()
-        adj = self._fields(self.adj)
-        i0, j0, bi, bj = self.box
-        box = _lib.Box2D(i0, j0, bi, bj)
-        seg_f = [[self._fields(self.seg[b, k]) for k in range(self.cp)] for b in range(2)]
-        ready = [torch.cuda.Event(), torch.cuda.Event()]  # buffer b holds its segment's states
-        free = [torch.cuda.Event(), torch.cuda.Event()]   # the sweep over buffer b has finished
-        side.wait_stream(main)  # the forward's checkpoints and the zeroing above come first
-
-        def recompute(c: int, b: int) -> list:
-            t_start = c * self.cp
-            L = min(self.cp, self.ns - t_start)
-            states = [self._fields(self.ckpt[c])] + seg_f[b][1:L]
-            for k in range(1, L):
-                rc = lib.fdtd2d_pass(C.byref(p), C.byref(states[k - 1]), C.byref(states[k]),
-                                     self.ez_scratch.data_ptr(), t_start + k - 1, 1, None, st_side)
-                if rc:
-                    raise _lib.FdtdError(rc, "fdtd2d_pass")
-            ready[b].record(side)
-            return states
-
-        order = list(reversed(range(self.ncp)))
-        states_of = {order[0]: recompute(order[0], 0)}
-        for idx, c in enumerate(order):
-            b = idx % 2
-            if idx + 1 < len(order):
-                nb = 1 - b
-                if idx >= 1:
-                    side.wait_event(free[nb])  # the sweep of the segment before used buffer nb
-                states_of[order[idx + 1]] = recompute(order[idx + 1], nb)
-            main.wait_event(ready[b])
-            states = states_of.pop(c)
-            t_start = c * self.cp
-            L = min(self.cp, self.ns - t_start)
-            for t in range(t_start + L, t_start, -1):
-                rc = lib.fdtd2d_adjoint_step(t, C.byref(p), C.byref(states[t - t_start - 1]), C.byref(adj),
-                                             self.tmp.data_ptr(), self.probe[0], self.probe[1], 2.0, box,
-                                             self.grad_naz.data_ptr(), None, st_main)
-                if rc:
-                    raise _lib.FdtdError(rc, "fdtd2d_adjoint_step")
-            free[b].record(main)
 
     def gradient_eps(self) -> torch.Tensor:
         """dJ/deps_r on the design box (float64): -naz^2 * dJ/dnaz."""

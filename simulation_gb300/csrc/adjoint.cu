@@ -14,8 +14,10 @@
 //   hx' = fy3*hx + fy2*(0.5*cx + fx1*ihx');  hy' = fx3*hy - fx2*(0.5*cy + fy1*ihy')
 // and the objective adds w/2 * ez[probe]^2 per step (J = sum ez^2 for w = 2).
 // Given the adjoints L' of x' this computes the adjoints L of x and adds
-// dJ/dnaz, dJ/dnbz on a design box.  Two kernels, because L(dz) at a cell
-// needs L'(dz) of its +i and +j neighbours after they received their E terms:
+// dJ/dnaz, dJ/dnbz on a design box.  L(dz) at a cell needs L'(dz) of its +i
+// and +j neighbours after they received their E terms, so the step is either
+// two kernels over the grid (fdtd2d_adjoint_step, in place) or one tiled
+// kernel with a one-cell halo of that temporary (k_adj_fused, out of place):
 //   A: recompute dz', ez at the cell from x; L(ez) from the H adjoints of the
 //      cell and its (i, j-1), (i-1, j) neighbours (+ probe seed); E backward;
 //      writes L'(dz)+E terms to a temporary and L(iz) in place; gradients;
@@ -35,7 +37,8 @@ struct AdjArgs {
   int src_kind, src_i, src_j;
   const float* src_table;
   fdtd2d_fields fwd;  // state before step t
-  fdtd2d_fields adj;  // adjoints: after step t in, before step t out
+  fdtd2d_fields adj;  // adjoints after step t (read)
+  fdtd2d_fields out;  // adjoints before step t (written; the same arrays as adj for the two-kernel step)
   float* tmp;
   int probe_i, probe_j;
   float probe_w;
@@ -63,10 +66,13 @@ __device__ __forceinline__ float lam_cy(const AdjArgs& a, int i, int j) {
   return __fmaf_rn(-__fmul_rn(0.5f, fx2), lhy, lihy_t);
 }
 
-__global__ void k_adj_a(const AdjArgs a) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= a.nx || j >= a.ny) return;
+// E part of the reverse step at one cell: recomputes dz' and ez from the
+// forward state, takes L(ez) from the H adjoints (+ the probe seed), runs the
+// E update backwards and returns T = L'(dz) + naz*L(ez~), the D adjoint
+// before the D update is undone.  With `own`, also writes L(iz) and adds the
+// cell's dJ/dnaz, dJ/dnbz (a cell computed only as a neighbour's halo does
+// neither).
+__device__ __forceinline__ float adj_e(const AdjArgs& a, int i, int j, bool own) {
   const size_t n = (size_t)i * a.ny + j;
   // forward recompute of dz' and ez at this cell (same formulas as the forward)
   float dzp = a.fwd.dz[n];
@@ -88,37 +94,38 @@ __global__ void k_adj_a(const AdjArgs a) {
   const float nbz = a.nbz ? __ldg(a.nbz + n) : 0.f;
   const float liz = a.nbz ? a.adj.iz[n] : 0.f;
   const float lezt = __fmaf_rn(nbz, liz, lez);
-  a.tmp[n] = __fmaf_rn(naz, lezt, a.adj.dz[n]);
-  if (a.nbz) a.adj.iz[n] = __fmaf_rn(-naz, lezt, liz);
-  const int bi = i - a.box.i0, bj = j - a.box.j0;
-  if (a.grad_naz && bi >= 0 && bi < a.box.ni && bj >= 0 && bj < a.box.nj) {
-    const size_t b = (size_t)bi * a.box.nj + bj;
-    a.grad_naz[b] = __fmaf_rn(lezt, diff, a.grad_naz[b]);
-    if (a.grad_nbz) a.grad_nbz[b] = __fmaf_rn(liz, ez, a.grad_nbz[b]);
+  if (own) {
+    if (a.nbz) a.out.iz[n] = __fmaf_rn(-naz, lezt, liz);
+    const int bi = i - a.box.i0, bj = j - a.box.j0;
+    if (a.grad_naz && bi >= 0 && bi < a.box.ni && bj >= 0 && bj < a.box.nj) {
+      const size_t b = (size_t)bi * a.box.nj + bj;
+      a.grad_naz[b] = __fmaf_rn(lezt, diff, a.grad_naz[b]);
+      if (a.grad_nbz) a.grad_nbz[b] = __fmaf_rn(liz, ez, a.grad_nbz[b]);
+    }
   }
+  return __fmaf_rn(naz, lezt, a.adj.dz[n]);
 }
 
 // cb*T at (i, j): the D adjoint flowing into the curl's H terms (0 where D is
 // not applied, or at a hard source whose dz' does not depend on the state)
-__device__ __forceinline__ float dgrad(const AdjArgs& a, int i, int j) {
+__device__ __forceinline__ float dgrad(const AdjArgs& a, int i, int j, float T) {
   if (i < 1 || j < 1 || i >= a.nx || j >= a.ny) return 0.f;
   if (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j) return 0.f;
   const float cb = __fmul_rn(__fmul_rn(__ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j)), 0.5f);
-  return __fmul_rn(cb, a.tmp[(size_t)i * a.ny + j]);
+  return __fmul_rn(cb, T);
 }
 
-__global__ void k_adj_b(const AdjArgs a) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= a.nx || j >= a.ny) return;
+// D and H part of the reverse step at one cell, given T there (T) and at
+// the (i+1, j) and (i, j+1) neighbours (Ti, Tj): L(dz) = ca*T, L(hy) +=
+// cb*T - cb[i+1]*T[i+1], L(hx) += -cb*T + cb[j+1]*T[j+1], then H backward.
+__device__ __forceinline__ void adj_dh(const AdjArgs& a, int i, int j, float T, float Ti, float Tj) {
   const size_t n = (size_t)i * a.ny + j;
   const bool hard_src = (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j);
-  const float T = a.tmp[n];
   float ldz;
   if (hard_src) ldz = 0.f;
   else if (i >= 1 && j >= 1) ldz = __fmul_rn(__fmul_rn(__ldg(a.pml.gx3 + i), __ldg(a.pml.gy3 + j)), T);
   else ldz = T;
-  const float dg = dgrad(a, i, j);
+  const float dg = dgrad(a, i, j, T);
   const bool hm = (i <= a.nx - 2) && (j <= a.ny - 2);
   float lhx = a.adj.hx[n], lhy = a.adj.hy[n], lihx = a.adj.ihx[n], lihy = a.adj.ihy[n];
   if (hm) {
@@ -128,16 +135,90 @@ __global__ void k_adj_b(const AdjArgs a) {
     lhx = __fmul_rn(__ldg(a.pml.fy3 + j), lhx);
     lhy = __fmul_rn(__ldg(a.pml.fx3 + i), lhy);
   }
-  lhy = __fadd_rn(__fadd_rn(lhy, dg), -dgrad(a, i + 1, j));
-  lhx = __fadd_rn(__fsub_rn(lhx, dg), dgrad(a, i, j + 1));
-  a.adj.dz[n] = ldz;
-  a.adj.hx[n] = lhx;
-  a.adj.hy[n] = lhy;
-  a.adj.ihx[n] = lihx;
-  a.adj.ihy[n] = lihy;
+  lhy = __fadd_rn(__fadd_rn(lhy, dg), -dgrad(a, i + 1, j, Ti));
+  lhx = __fadd_rn(__fsub_rn(lhx, dg), dgrad(a, i, j + 1, Tj));
+  a.out.dz[n] = ldz;
+  a.out.hx[n] = lhx;
+  a.out.hy[n] = lhy;
+  a.out.ihx[n] = lihx;
+  a.out.ihy[n] = lihy;
+}
+
+// Two-kernel form (in place, T through a full-grid temporary)
+__global__ void k_adj_a(const AdjArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  a.tmp[(size_t)i * a.ny + j] = adj_e(a, i, j, true);
+}
+
+__global__ void k_adj_b(const AdjArgs a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= a.nx || j >= a.ny) return;
+  const size_t n = (size_t)i * a.ny + j;
+  const float Ti = (i + 1 < a.nx) ? a.tmp[n + a.ny] : 0.f;
+  const float Tj = (j + 1 < a.ny) ? a.tmp[n + 1] : 0.f;
+  adj_dh(a, i, j, a.tmp[n], Ti, Tj);
+}
+
+// Fused form: one block takes a TI x TJ tile, computes T on the tile plus
+// one row and one column of halo into shared memory, then runs the D/H part
+// for the tile.  It reads the adjoints after step t (a.adj) and writes those
+// before it to other arrays (a.out): a halo cell's inputs belong to the
+// neighbouring tile, which must not have overwritten them.  Same per-cell
+// arithmetic as the two-kernel form, so the results are bitwise equal.
+constexpr int kAdjTJ = 32, kAdjTI = 8;
+__global__ void __launch_bounds__(kAdjTJ * kAdjTI) k_adj_fused(const AdjArgs a) {
+  __shared__ float sT[kAdjTI + 1][kAdjTJ + 1];
+  const int j0 = blockIdx.x * kAdjTJ, i0 = blockIdx.y * kAdjTI;
+  const int tid = threadIdx.y * kAdjTJ + threadIdx.x;
+  for (int idx = tid; idx < (kAdjTI + 1) * (kAdjTJ + 1); idx += kAdjTI * kAdjTJ) {
+    const int li = idx / (kAdjTJ + 1), lj = idx - li * (kAdjTJ + 1);
+    const int i = i0 + li, j = j0 + lj;
+    float T = 0.f;
+    if (i < a.nx && j < a.ny) T = adj_e(a, i, j, li < kAdjTI && lj < kAdjTJ);
+    sT[li][lj] = T;
+  }
+  __syncthreads();
+  const int i = i0 + threadIdx.y, j = j0 + threadIdx.x;
+  if (i >= a.nx || j >= a.ny) return;
+  adj_dh(a, i, j, sT[threadIdx.y][threadIdx.x], sT[threadIdx.y + 1][threadIdx.x], sT[threadIdx.y][threadIdx.x + 1]);
 }
 
 }  // namespace
+
+// One reverse step in one launch (k_adj_fused): adjoints after step t from
+// adj_in, before it to adj_out (distinct arrays), fwd = the state before t.
+int launch_adjoint_fused(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd, const fdtd2d_fields& adj_in,
+                         const fdtd2d_fields& adj_out, int probe_i, int probe_j, float probe_w,
+                         const fdtd2d_box& box, float* grad_naz, float* grad_nbz, cudaStream_t st) {
+  AdjArgs a{};
+  a.nx = p.nx;
+  a.ny = p.ny;
+  a.t = t;
+  a.pml = p.pml;
+  a.naz = p.naz;
+  a.nbz = p.nbz;
+  a.src_kind = p.src.kind;
+  a.src_i = p.src.i;
+  a.src_j = p.src.j;
+  a.src_table = p.src.table;
+  a.fwd = fwd;
+  a.adj = adj_in;
+  a.out = adj_out;
+  a.tmp = nullptr;
+  a.probe_i = probe_i;
+  a.probe_j = probe_j;
+  a.probe_w = probe_w;
+  a.box = box;
+  a.grad_naz = grad_naz;
+  a.grad_nbz = grad_nbz;
+  const dim3 blk(kAdjTJ, kAdjTI);
+  const dim3 grd((p.ny + kAdjTJ - 1) / kAdjTJ, (p.nx + kAdjTI - 1) / kAdjTI);
+  k_adj_fused<<<grd, blk, 0, st>>>(a);
+  return fdtd_host::check_launch();
+}
 
 }  // namespace fdtd
 
@@ -187,6 +268,7 @@ int fdtd2d_adjoint_step(int t, const fdtd2d_params* p, const fdtd2d_fields* fwd,
   a.src_table = p->src.table;
   a.fwd = *fwd;
   a.adj = *adj;
+  a.out = *adj;
   a.tmp = adj_tmp;
   a.probe_i = probe_i;
   a.probe_j = probe_j;

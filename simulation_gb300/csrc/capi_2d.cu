@@ -254,8 +254,13 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
   for (size_t i = 0; i < sched.size(); ++i) {
     const FieldSet& in = (i % 2 == 0) ? user : ws;
     const FieldSet& out = (i % 2 == 0) ? ws : user;
+    // the last pass alone tests the fields it writes for Inf/NaN: a non-finite
+    // value never turns finite again under the update (every operation on
+    // Inf/NaN yields Inf/NaN, and it spreads to the neighbours each step), so
+    // that one test sees anything an earlier pass would have
+    int* status = (i + 1 == sched.size()) ? s->status : nullptr;
     if (!ext_on(p)) {
-      rc = launch_march(*p, in, out, s->ez, t, sched[i], s->status, s->probe_ez, st);
+      rc = launch_march(*p, in, out, s->ez, t, sched[i], status, s->probe_ez, st);
     } else {
       if (p->tfsf_npml > 0) {
         if (t + sched[i] > line_t0 + line_n) {  // next chunk of whole passes
@@ -268,7 +273,7 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
         ext.inc_e = inc_e + (size_t)(t - line_t0) * p->ny;
         ext.inc_h = inc_h + (size_t)(t - line_t0) * 2;
       }
-      rc = launch_march_ext(*p, in, out, s->ez, t, sched[i], s->status, ext, st);
+      rc = launch_march_ext(*p, in, out, s->ez, t, sched[i], status, ext, st);
     }
     if (rc) return rc;
     t += sched[i];

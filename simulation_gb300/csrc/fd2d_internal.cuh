@@ -36,6 +36,14 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
                  int* status, float* probe_ez, cudaStream_t st);
 // columns a warp of the fused kernel owns (for workspace/grid sizing)
 int march_max_steps_per_pass();
+// A pass that also records the state after each of its steps (the adjoint's
+// recompute): rec[s] receives dz, iz, hx, hy after step t0+s+1, s < k.
+// Point source only, with PML (plain kernels, 64-column stripes).
+struct RecSet {
+  float *dz, *iz, *hx, *hy;
+};
+int launch_march_record(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out, float* ez, int t0, int k,
+                        const RecSet* rec, cudaStream_t st);
 
 // The fd2d_3_4 extras inside a fused pass (fd2d/python/fd2d_3_4.py:90-170):
 // the TF/SF box corrections (inctdz, incthx, incthy) from a precomputed

@@ -62,6 +62,7 @@ MarchArgs march_args(const fdtd2d_params& p, const FieldSet& in, const FieldSet&
   a.probe_i = p.probe_i;
   a.probe_j = p.probe_j;
   a.probe_ez = probe_ez;
+  a.pml_hint = has_pml(p) ? p.pml_cells : 0;
   return a;
 }
 }  // namespace
@@ -93,7 +94,10 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
   const MarchArgs a = march_args(p, in, out, ez, t0, status, probe_ez);
   const bool lossy = p.nbz != nullptr;
   const bool pml = has_pml(p);
-  int cpl = g_cfg.cpl ? g_cfg.cpl : (k >= 3 ? 2 : 4);
+  // 128-column stripes unless the grid is too small to fill the GPU with
+  // them (with the interior iterations they beat 64-column stripes at K = 4:
+  // 386 against 350 Gcell/s at 8192^2)
+  int cpl = g_cfg.cpl ? g_cfg.cpl : 4;
   if (!g_cfg.cpl && cpl == 4 && k >= 1 && k <= HALO) {
     // small grids: if 128-column stripes times the shortest segments would not
     // fill one wave of warps (32 per SM), use 64-column stripes instead
@@ -108,6 +112,25 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
   return launch_cpl<4>(a, k, lossy, pml, st);
 }
 
+int launch_march_record(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out, float* ez, int t0, int k,
+                        const RecSet* rec, cudaStream_t st) {
+  if (!has_pml(p) || k < 1 || k > HALO) return FDTD_ERR_UNSUPPORTED;
+  MarchArgs a = march_args(p, in, out, ez, t0, nullptr, nullptr);
+  for (int s = 0; s < k; ++s) a.rec[s] = rec[s];
+  const bool lossy = p.nbz != nullptr;
+  auto go = [&](auto kk) -> int {
+    constexpr int K = decltype(kk)::value;
+    if (lossy) return launch_t<K, 2, true, true, kTraceRecord>(a, g_cfg.warps, g_cfg.seg_rows, st);
+    return launch_t<K, 2, false, true, kTraceRecord>(a, g_cfg.warps, g_cfg.seg_rows, st);
+  };
+  switch (k) {
+    case 1: return go(std::integral_constant<int, 1>{});
+    case 2: return go(std::integral_constant<int, 2>{});
+    case 3: return go(std::integral_constant<int, 3>{});
+    default: return go(std::integral_constant<int, 4>{});
+  }
+}
+
 }  // namespace fdtd
 
 extern "C" int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, int seg_rows) {
@@ -116,5 +139,11 @@ extern "C" int fdtd2d_set_march_config(int cols_per_lane, int warps_per_block, i
   fdtd::march::g_cfg.cpl = cols_per_lane;
   fdtd::march::g_cfg.warps = warps_per_block;
   fdtd::march::g_cfg.seg_rows = seg_rows;
+  return FDTD_OK;
+}
+
+extern "C" int fdtd2d_set_march_balance(float gen_cost) {
+  if (gen_cost != 0.f && (!(gen_cost >= 1.f) || gen_cost > 16.f)) return FDTD_ERR_ARG;
+  fdtd::march::g_cfg.gen_cost = gen_cost;
   return FDTD_OK;
 }

@@ -43,6 +43,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 
 #include "fd2d_internal.cuh"
 
@@ -55,6 +56,8 @@ constexpr int HALO = 4;  // halo columns on each side (>= K, multiple of 4 for a
 constexpr int kPlain = -2;        // NFC of the kernels without the fd2d_3_4 extras
 constexpr int kExtMinBlocks = 3;  // blocks per SM the extras kernels are held to
 constexpr bool kPlainPrefetch = true;  // the plain kernels prefetch rows too (false: direct loads)
+constexpr int kWarps = 4;              // warps per block of every fused kernel
+constexpr int kTraceNone = 0, kTraceProbe = 1, kTraceRecord = 2;  // what a plain pass keeps besides its output
 
 struct MarchArgs {
   int nx, ny;
@@ -67,11 +70,19 @@ struct MarchArgs {
   const float* src_table;
   int t0;
   int seg_rows, n_stripes, n_segs;
+  // plain kernels: the n_gen_lo + n_gen_hi stripes at the grid's left and
+  // right edges (which the absorbing layer or the grid boundary make general)
+  // have their own, shorter segments (seg_rows_g rows, n_segs_g of them); the
+  // other stripes' first and last segments are seg_first rows, the rest
+  // seg_rows.  Only the balance of the one wave of warps depends on this.
+  int n_gen_lo, n_gen_hi, seg_rows_g, n_segs_g, seg_first;
   int* status;
   int check_finite;
   int probe_i, probe_j;  // Ez trace cell (probe_ez != nullptr)
   float* probe_ez;       // probe_ez[t-1] = ez at the probe after step t
   MarchExt ext;          // TF/SF corrections and the running DFT (EXT kernels)
+  RecSet rec[HALO];      // recording passes: rec[s] <- dz, iz, hx, hy after step t0+s+1
+  int pml_hint;          // absorbing-layer thickness in cells if known (host: work layout only)
 };
 
 // Shared memory per warp beyond the PML columns, in floats (each part a
@@ -87,11 +98,22 @@ __host__ __device__ constexpr int ext_dft_floats(int k, int nf) {
 __host__ __device__ constexpr int ext_warp_floats(int k, int nf, bool lossy, bool pml, int w) {
   return ext_dft_floats(k, nf) + 2 * ext_nfields(lossy, pml) * w + (k + 1) * (lossy ? 2 : 1) * w;
 }
+// dynamic shared memory of a block of `warps` warps with w-column stripes:
+// the PML column coefficients (5 rows of w) and the rings above, per warp
+__host__ __device__ constexpr size_t march_smem_bytes(int warps, int k, int nf, bool lossy, bool pml, int w,
+                                                     bool prefetch) {
+  return (size_t)warps * ((pml ? 5 * w : 0) + (prefetch ? ext_warp_floats(k, nf, lossy, pml, w) : 0)) * sizeof(float);
+}
 
 struct MarchConfig {
   int cpl = 0;       // columns per lane; 0 = automatic (measured best: 4 for K <= 2, 2 for K >= 3)
   int warps = 4;
   int seg_rows = 0;  // 0 = automatic
+  // time of a general row iteration over an interior one (load balance);
+  // 0 = the measured best for the stripe width: 8192^2 K = 4 lossy PML,
+  // 128-column stripes 386 Gcell/s at 3.5-5 (297 at 2, 349 at 8), 64-column
+  // stripes 350 at 2.5 (338 at 3)
+  float gen_cost = 0.f;
 };
 
 extern MarchConfig g_cfg;  // tuning knob (fdtd2d_set_march_config)
@@ -245,8 +267,24 @@ __device__ __forceinline__ void pf_dft(const MarchArgs& a, float* rg, int row, i
 // itself is compiled only into the body that warps touching a TF/SF edge run
 // (TF = true: a stripe with an edge column, or rows reaching an edge row);
 // the others run the body without it.
-template <int K, int CPL, bool LOSSY, bool PML, int WARPS, bool PROBE, int NFC, bool TF>
-__device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_x, const int i_s_x, const int i_e_x) {
+// One row iteration of a warp's march, in two forms sharing the same register
+// state:
+//   * the general form (GEN) handles every case: PML coefficients per row and
+//     column, the grid's first/last rows and columns (the reference loops'
+//     bounds), the point source, the probe trace and the TF/SF edges;
+//   * the interior form (INT) runs where none of these can occur in any row
+//     the iteration touches (rows r-K .. r) nor in the warp's columns: unit
+//     PML coefficients (d_update_unit / h_update_pml_unit give the same values
+//     as the general formulas there), no bounds tests, no source or probe
+//     test.  It cuts the per-cell work roughly in half.
+// The warp decides per iteration, on warp-uniform data: its columns are
+// classified once (cint), its rows 32 at a time by a ballot over the lanes
+// (one row per lane, see row_ok) into `run`, the count of good rows ending at
+// the row entering level 1.  An iteration is interior when cint and run > K.
+template <int K, int CPL, bool LOSSY, bool PML, int WARPS, int TRACE, int NFC, bool TF>
+__device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe, const int i_s, const int i_e) {
+  constexpr bool PROBE = TRACE == kTraceProbe;  // Ez at one cell every step
+  constexpr bool REC = TRACE == kTraceRecord;   // dz, iz, hx, hy after every step
   constexpr bool EXT = NFC != kPlain;
   constexpr bool TFS = EXT && TF;  // this body applies the TF/SF edge corrections
   constexpr bool PF = EXT || kPlainPrefetch;  // rows prefetched by cp.async into shared rings
@@ -255,7 +293,7 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
   constexpr int W = 32 * CPL;
   constexpr int OUTW = W - 2 * HALO;
   static_assert(K >= 1 && K <= HALO, "steps per pass must not exceed the halo");
-  static_assert(!(EXT && PROBE), "the probe trace is not kept by EXT kernels");
+  static_assert(!(EXT && TRACE != kTraceNone), "the probe trace and the records are not kept by EXT kernels");
   // per warp: gy2, gy3, fy1, fy2, fy3 of its columns (PML); then (nf > 0)
   // the DFT ring [K+1 rows][32 lanes][nf][re0, re1, im0, im1] (lane stride
   // padded to an odd number of 16-byte units: conflict-free vector access)
@@ -266,15 +304,9 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
 
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
-  // plain kernels map warp -> (stripe, segment) here; EXT kernels get it
-  // from k_march (stripe_x, rows i_s_x .. i_e_x-1)
-  const int gw = blockIdx.x * WARPS + wid;
-  const int stripe = EXT ? stripe_x : gw % a.n_stripes;
-  const int seg = gw / a.n_stripes;
-  if (!EXT && seg >= a.n_segs) return;  // whole warp leaves; nothing below syncs the block
-
   const int nx = a.nx, ny = a.ny;
-  const int j0 = stripe * OUTW - HALO + lane * CPL;  // first column of this lane (multiple of 4 or 2)
+  const int jw0 = stripe * OUTW - HALO;              // first column of the warp's stripe
+  const int j0 = jw0 + lane * CPL;                   // first column of this lane (multiple of 4 or 2)
   const bool vin = (j0 >= 0) && (j0 + CPL <= ny);    // ny % 4 == 0: a vector is wholly in or out
   const bool vout = vin && (lane * CPL >= HALO) && (lane * CPL < HALO + OUTW);
 
@@ -293,19 +325,31 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
   float* const tw = ring + M * 32 * ls;
   float* const fring = ring + ext_dft_floats(K, nf) + lane * CPL;  // [2][NFA][W], this lane's columns
   float* const mring = fring + 2 * NFA * W;                         // [M][NMA][W]
+  // columns: interior if every column of the stripe lies in 1 .. ny-2 with
+  // unit PML coefficients, and neither the source nor the probe is among them
+  bool col_ok = (j0 >= 1) && (j0 + CPL - 1 <= ny - 2);
   if (PML) {
 #pragma unroll
     for (int c = 0; c < CPL; ++c) {
       const int j = j0 + c;
       const bool ok = (j >= 0) && (j < ny);
-      cg[0 * W + c] = ok ? __ldg(a.pml.gy2 + j) : 1.f;
-      cg[1 * W + c] = ok ? __ldg(a.pml.gy3 + j) : 1.f;
-      cg[2 * W + c] = ok ? __ldg(a.pml.fy1 + j) : 0.f;
-      cg[3 * W + c] = ok ? __ldg(a.pml.fy2 + j) : 1.f;
-      cg[4 * W + c] = ok ? __ldg(a.pml.fy3 + j) : 1.f;
+      const float gy2 = ok ? __ldg(a.pml.gy2 + j) : 1.f;
+      const float gy3 = ok ? __ldg(a.pml.gy3 + j) : 1.f;
+      const float fy1 = ok ? __ldg(a.pml.fy1 + j) : 0.f;
+      const float fy2 = ok ? __ldg(a.pml.fy2 + j) : 1.f;
+      const float fy3 = ok ? __ldg(a.pml.fy3 + j) : 1.f;
+      cg[0 * W + c] = gy2;
+      cg[1 * W + c] = gy3;
+      cg[2 * W + c] = fy1;
+      cg[3 * W + c] = fy2;
+      cg[4 * W + c] = fy3;
+      col_ok &= gy2 == 1.f && gy3 == 1.f && fy1 == 0.f && fy2 == 1.f && fy3 == 1.f;
     }
     __syncwarp();
   }
+  const bool src_here = a.src_kind != FDTD_SRC_NONE && a.src_j >= jw0 && a.src_j < jw0 + W;
+  const bool probe_here = PROBE && a.probe_j >= jw0 && a.probe_j < jw0 + W;
+  const bool cint = !TFS && __all_sync(FULL, col_ok);
   if constexpr (DFT) {
     for (int x = lane; x < K * nf; x += 32) {
       const int s = x / nf, f = x - s * nf;
@@ -330,6 +374,19 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
       if (j == ny - np) tcol |= 8u << (4 * c);
     }
   }
+  // rows: bit l of row_ok(b) says row b+l may be touched by an interior
+  // iteration (1 .. nx-2, unit PML row coefficients, not the source's or the
+  // probe's row when its column is in the stripe)
+  auto row_ok = [&](int b) -> unsigned {
+    const int row = b + lane;
+    bool g = row >= 1 && row <= nx - 2;
+    if (PML && g)
+      g = __ldg(a.pml.gx2 + row) == 1.f && __ldg(a.pml.gx3 + row) == 1.f && __ldg(a.pml.fx1 + row) == 0.f &&
+          __ldg(a.pml.fx2 + row) == 1.f && __ldg(a.pml.fx3 + row) == 1.f;
+    if (src_here && row == a.src_i) g = false;
+    if (probe_here && row == a.probe_i) g = false;
+    return __ballot_sync(FULL, g);
+  };
 
   // level state: values of the row each level will complete next
   float p_hy[K][CPL], p_hx[K][CPL], p_ihx[K][CPL], p_ihy[K][CPL], p_ez[K][CPL], p_dz[K][CPL], p_iz[K][CPL];
@@ -341,8 +398,6 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
       p_ez[s][c] = p_dz[s][c] = p_iz[s][c] = 0.f;
     }
 
-  const int i_s = EXT ? i_s_x : seg * a.seg_rows;
-  const int i_e = EXT ? i_e_x : min(nx, i_s + a.seg_rows);
   const int r_begin = max(0, i_s - K);
   const int r_end = i_e - 1 + K;
   bool finite_ok = true;
@@ -362,8 +417,16 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
                               ncell, nf);
     cp_async_commit();
   }
+  // good-row run before the first iteration (rows r_begin-K .. r_begin-1)
+  int gbase = r_begin - K;
+  unsigned gmask = cint ? row_ok(gbase) : 0u;
+  int run = 0;
+  if (cint)
+    for (int q = r_begin - K; q < r_begin; ++q) run = ((gmask >> (q - gbase)) & 1u) ? run + 1 : 0;
 
-  for (int r = r_begin; r <= r_end; ++r) {
+  // one row iteration: row r enters level 1, level s completes row r-s-1
+  auto iterate = [&](const int r, auto int_tag) {
+    constexpr bool INT = decltype(int_tag)::value;
     float in_dz[CPL], in_iz[CPL], in_hx[CPL], in_hy[CPL], in_ihx[CPL], in_ihy[CPL];
     if constexpr (PF) {
       // row r+1 starts its way in; row r's copies (issued one iteration ago) complete
@@ -430,7 +493,7 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
         if (LOSSY) ld_row<CPL>(a.nbz + off, ok, nbz);
       }
       float gx3q = 1.f, gx2q = 1.f;
-      if (PML && qok) {
+      if (!INT && PML && qok) {
         gx3q = __ldg(a.pml.gx3 + q);
         gx2q = __ldg(a.pml.gx2 + q);
       }
@@ -447,21 +510,25 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
 #pragma unroll
       for (int c = 0; c < CPL; ++c) {
         const int j = j0 + c;
+        const float hxm = (c == 0) ? hx_left : in_hx[c - 1];
         float d = in_dz[c];
-        if (drow && j >= 1 && j < ny) {
-          const float hxm = (c == 0) ? hx_left : in_hx[c - 1];
-          const float gy2 = PML ? cg[0 * W + c] : 1.f;
-          const float gy3 = PML ? cg[1 * W + c] : 1.f;
-          d = d_update(d, in_hy[c], p_hy[s][c], in_hx[c], hxm, gx3q, gy3, gx2q, gy2);
-        }
-        if (a.src_kind != FDTD_SRC_NONE && q == a.src_i && j == a.src_j) {
-          const float v = __ldg(a.src_table + a.t0 + s);
-          d = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(d, v);
-        }
-        if (TFS) {
-          const float d_lo = __fmaf_rn(0.5f, hxi_lo, d), d_hi = __fmaf_rn(-0.5f, hxi_hi, d);
-          d = (d_tf && (tcol & (1u << (4 * c)))) ? d_lo : d;
-          d = (d_tf && (tcol & (2u << (4 * c)))) ? d_hi : d;
+        if constexpr (INT) {
+          d = d_update_unit(d, in_hy[c], p_hy[s][c], in_hx[c], hxm);
+        } else {
+          if (drow && j >= 1 && j < ny) {
+            const float gy2 = PML ? cg[0 * W + c] : 1.f;
+            const float gy3 = PML ? cg[1 * W + c] : 1.f;
+            d = d_update(d, in_hy[c], p_hy[s][c], in_hx[c], hxm, gx3q, gy3, gx2q, gy2);
+          }
+          if (a.src_kind != FDTD_SRC_NONE && q == a.src_i && j == a.src_j) {
+            const float v = __ldg(a.src_table + a.t0 + s);
+            d = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(d, v);
+          }
+          if (TFS) {
+            const float d_lo = __fmaf_rn(0.5f, hxi_lo, d), d_hi = __fmaf_rn(-0.5f, hxi_hi, d);
+            d = (d_tf && (tcol & (1u << (4 * c)))) ? d_lo : d;
+            d = (d_tf && (tcol & (2u << (4 * c)))) ? d_hi : d;
+          }
         }
         float izv = in_iz[c];
         const float e = LOSSY ? e_update_lossy(d, izv, naz[c], nbz[c]) : e_update(d, naz[c]);
@@ -470,7 +537,8 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
         ne[c] = e;
         // the probe cell's Ez is recorded by the warp that owns it (output
         // column, row inside the segment), where every level is valid
-        if (PROBE && q == a.probe_i && j == a.probe_j && vout && q >= i_s && q < i_e) a.probe_ez[a.t0 + s] = e;
+        if (!INT && PROBE && q == a.probe_i && j == a.probe_j && vout && q >= i_s && q < i_e)
+          a.probe_ez[a.t0 + s] = e;
       }
 
       // ---- running DFT of row q at step t0+s+1 (stored where owned)
@@ -518,7 +586,7 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
         ld_row<CPL>(erow + (vin ? j0 : 0), vin && hy_tf, ezr);
       }
       float fx1 = 0.f, fx2 = 1.f, fx3 = 1.f;
-      if (PML && hrow) {
+      if (!INT && PML && hrow) {
         fx1 = __ldg(a.pml.fx1 + qc);
         fx2 = __ldg(a.pml.fx2 + qc);
         fx3 = __ldg(a.pml.fx3 + qc);
@@ -528,8 +596,13 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
       for (int c = 0; c < CPL; ++c) {
         const int j = j0 + c;
         float hxv = p_hx[s][c], hyv = p_hy[s][c], ihxv = p_ihx[s][c], ihyv = p_ihy[s][c];
-        if (hrow && j >= 0 && j <= ny - 2) {
-          const float er = (c == CPL - 1) ? ez_right : p_ez[s][c + 1];
+        const float er = (c == CPL - 1) ? ez_right : p_ez[s][c + 1];
+        if constexpr (INT) {
+          if (PML)
+            h_update_pml_unit(p_ez[s][c], er, ne[c], hxv, hyv, ihxv, ihyv);
+          else
+            h_update_free(p_ez[s][c], er, ne[c], hxv, hyv);
+        } else if (hrow && j >= 0 && j <= ny - 2) {
           if (PML)
             h_update_pml(p_ez[s][c], er, ne[c], hxv, hyv, ihxv, ihyv, fx1, fx2, fx3, cg[2 * W + c], cg[3 * W + c],
                          cg[4 * W + c]);
@@ -547,6 +620,16 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
         ohy[c] = hyv;
         oihx[c] = ihxv;
         oihy[c] = ihyv;
+      }
+
+      // ---- recording passes store every level's completed row: the state
+      //      after step t0+s+1 (the values level K stores for s = K-1)
+      if (REC && vout && qc >= i_s && qc < i_e) {
+        const size_t off = (size_t)qc * ny + j0;
+        st_row<CPL>(a.rec[s].dz + off, p_dz[s]);
+        if (LOSSY) st_row<CPL>(a.rec[s].iz + off, p_iz[s]);
+        st_row<CPL>(a.rec[s].hx + off, ohx);
+        st_row<CPL>(a.rec[s].hy + off, ohy);
       }
 
       // ---- level K stores its completed row
@@ -590,6 +673,22 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe_
       }
     }
     if constexpr (PF) mk = (mk + 1 == M) ? 0 : mk + 1;
+  };
+
+  for (int r = r_begin; r <= r_end; ++r) {
+    bool interior = false;
+    if (cint) {
+      if (r - gbase >= 32) {
+        gbase += 32;
+        gmask = row_ok(gbase);
+      }
+      run = ((gmask >> (r - gbase)) & 1u) ? run + 1 : 0;
+      interior = run > K;  // rows r-K .. r all good
+    }
+    if (interior)
+      iterate(r, std::true_type{});
+    else
+      iterate(r, std::false_type{});
   }
   if constexpr (PF) cp_async_wait_all();  // the copies of row r_end+1 land before the warp leaves
   if (a.check_finite && __any_sync(FULL, !finite_ok) && lane == 0) raise_status(a.status, ST_NONFINITE);
@@ -613,6 +712,31 @@ __host__ __device__ inline bool tf_segment(int np, int nx, int seg_rows, int seg
   return (np - 2 >= r0 && np - 2 <= r1) || (nx - np >= r0 && nx - np <= r1);
 }
 
+// Warp -> work of the plain kernels (layout: plain_layout): warps
+// 0 .. n_int*n_segs-1 take the stripes away from the edges, the rest the
+// general stripes at either edge with their shorter segments.  False: no work.
+__host__ __device__ inline bool plain_work(const MarchArgs& a, int gw, int& stripe, int& i_s, int& i_e) {
+  const int n_int = a.n_stripes - a.n_gen_lo - a.n_gen_hi;
+  const int n_main = n_int * a.n_segs;
+  if (gw < n_main) {
+    stripe = a.n_gen_lo + gw % n_int;
+    const int seg = gw / n_int;
+    i_s = seg == 0 ? 0 : a.seg_first + (seg - 1) * a.seg_rows;
+    i_e = (seg == a.n_segs - 1) ? a.nx : (seg == 0 ? a.seg_first : i_s + a.seg_rows);
+  } else {
+    const int n_gen = a.n_gen_lo + a.n_gen_hi;
+    if (n_gen == 0) return false;
+    const int k = gw - n_main;
+    const int g = k % n_gen, seg = k / n_gen;
+    if (seg >= a.n_segs_g) return false;
+    stripe = g < a.n_gen_lo ? g : a.n_stripes - n_gen + g;
+    i_s = seg * a.seg_rows_g;
+    i_e = i_s + a.seg_rows_g;
+  }
+  i_e = i_e < a.nx ? i_e : a.nx;
+  return i_s < i_e;
+}
+
 __device__ __forceinline__ int pick6(const int (&v)[6], int i) {  // v[i] without a local-memory copy
   return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : i == 3 ? v[3] : i == 4 ? v[4] : v[5];
 }
@@ -622,13 +746,15 @@ __device__ __forceinline__ int pick6(const int (&v)[6], int i) {  // v[i] withou
 // half there and the warps after them take the second halves, first the edge
 // stripes' segments (nc * n_segs), then the edge segments of the other
 // stripes ((n_stripes - nc) * nr).
-template <int K, int CPL, bool LOSSY, bool PML, int WARPS, bool PROBE, int NFC>
+template <int K, int CPL, bool LOSSY, bool PML, int WARPS, int TRACE, int NFC>
 __global__ void __launch_bounds__(WARPS * 32, CPL == 2 ? (NFC == kPlain ? 4 : kExtMinBlocks) : 1)
     k_march(const MarchArgs a) {
   const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
   const int n_base = a.n_stripes * a.n_segs;
   if constexpr (NFC == kPlain) {
-    march_body<K, CPL, LOSSY, PML, WARPS, PROBE, NFC, false>(a, 0, 0, 0);
+    int stripe, i_s, i_e;
+    if (!plain_work(a, gw, stripe, i_s, i_e)) return;  // whole warp leaves; nothing below syncs the block
+    march_body<K, CPL, LOSSY, PML, WARPS, TRACE, NFC, false>(a, stripe, i_s, i_e);
   } else {
     const int np = a.ext.tfsf_npml;
     const int nc = a.ext.nc, nr = a.ext.nr;
@@ -660,25 +786,65 @@ __global__ void __launch_bounds__(WARPS * 32, CPL == 2 ? (NFC == kPlain ? 4 : kE
     if (half == 2) i_s = mid;
     if (i_s >= i_e) return;
     if (tf)
-      march_body<K, CPL, LOSSY, PML, WARPS, PROBE, NFC, true>(a, stripe, i_s, i_e);
+      march_body<K, CPL, LOSSY, PML, WARPS, TRACE, NFC, true>(a, stripe, i_s, i_e);
     else
-      march_body<K, CPL, LOSSY, PML, WARPS, PROBE, NFC, false>(a, stripe, i_s, i_e);
+      march_body<K, CPL, LOSSY, PML, WARPS, TRACE, NFC, false>(a, stripe, i_s, i_e);
   }
 }
 
-template <int K, int CPL, bool LOSSY, bool PML, bool PROBE, int NFC = kPlain>
+// Work layout of the plain kernels' single wave of warps (MarchArgs).  The
+// stripes that reach column 0, column ny-1 or (with the pml_hint) the
+// absorbing layer run general iterations throughout; they get gen_cost times
+// as many segments.  In the other stripes only the rows of the layer and the
+// grid's first/last rows (plus the K-row cone) iterate in the general form,
+// so their first and last segments are shortened by that extra time.
+template <int K, int CPL>
+long plain_layout(MarchArgs& a, long resident, float G) {
+  constexpr int W = 32 * CPL, OUTW = W - 2 * HALO;
+  const int P = a.pml_hint > 0 ? a.pml_hint : 0;
+  auto general = [&](int s) {
+    const int lo = s * OUTW - HALO, hi = lo + W - 1;
+    return lo < std::max(P, 1) || hi > a.ny - 2 - P;
+  };
+  int glo = 0, ghi = 0;
+  while (glo < a.n_stripes && general(glo)) ++glo;
+  while (ghi < a.n_stripes - glo && general(a.n_stripes - 1 - ghi)) ++ghi;
+  const int n_int = a.n_stripes - glo - ghi, n_gen = glo + ghi;
+  const int mn = min_seg_rows(K);
+  if (!(G >= 1.f)) G = 1.f;
+  long n_segs = (long)((double)resident / ((double)n_int + (double)G * n_gen));
+  if (n_segs < 1) n_segs = 1;
+  const long n_segs_g = std::max(1L, (long)(G * n_segs));
+  const int rg = std::max((int)((a.nx + n_segs_g - 1) / n_segs_g), mn);
+  a.seg_rows_g = rg;
+  a.n_segs_g = (a.nx + rg - 1) / rg;
+  const int T = (int)((G - 1.f) * (float)(P + K + 1));
+  int L = a.nx, f = a.nx, ns = 1;
+  if (n_segs > 1) {
+    L = std::max((int)((a.nx + 2L * T + n_segs - 1) / n_segs), mn);
+    f = std::min(std::max(L - T, mn), a.nx);
+    ns = a.nx <= f ? 1 : 1 + (a.nx - f + L - 1) / L;
+  }
+  a.seg_rows = L;
+  a.seg_first = f;
+  a.n_segs = ns;
+  a.n_gen_lo = glo;
+  a.n_gen_hi = ghi;
+  return (long)n_int * ns + (long)n_gen * a.n_segs_g;
+}
+
+template <int K, int CPL, bool LOSSY, bool PML, int TRACE, int NFC = kPlain>
 int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
-  constexpr int WARPS = 4;
+  constexpr int WARPS = kWarps;
   (void)warps_cfg;
   MarchArgs a = a0;
   constexpr int W = 32 * CPL;
   constexpr int OUTW = W - 2 * HALO;
-  auto kern = k_march<K, CPL, LOSSY, PML, WARPS, PROBE, NFC>;
+  auto kern = k_march<K, CPL, LOSSY, PML, WARPS, TRACE, NFC>;
   constexpr bool EXT = NFC != kPlain;
   constexpr bool PF = EXT || kPlainPrefetch;
   const int nf = NFC >= 0 ? NFC : (EXT ? a.ext.nf : 0);
-  const size_t smem =
-      (size_t)WARPS * ((PML ? 5 * W : 0) + (PF ? ext_warp_floats(K, nf, LOSSY, PML, W) : 0)) * sizeof(float);
+  const size_t smem = march_smem_bytes(WARPS, K, nf, LOSSY, PML, W, PF);
   if (smem > 48 * 1024) {
     const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) {
@@ -688,13 +854,14 @@ int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
   }
   a.n_stripes = (a.ny + OUTW - 1) / OUTW;
   int seg_rows = seg_cfg;
+  long resident = 0;
   if (seg_rows <= 0) {
     int dev = 0, nsm = 0, blocks_per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, WARPS * 32, smem);
     if (blocks_per_sm < 1) blocks_per_sm = 1;
-    const long resident = (long)nsm * blocks_per_sm * WARPS;
+    resident = (long)nsm * blocks_per_sm * WARPS;
     // one wave of warps: n_stripes * n_segs ~= resident warps
     long n_segs = resident / a.n_stripes;
     if (EXT && a.ext.tfsf_npml > 0) {
@@ -711,7 +878,13 @@ int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
   }
   a.seg_rows = seg_rows;
   a.n_segs = (a.nx + seg_rows - 1) / seg_rows;
+  a.seg_first = seg_rows;
+  a.n_gen_lo = a.n_gen_hi = 0;
+  a.seg_rows_g = seg_rows;
+  a.n_segs_g = 0;
   long warps = (long)a.n_stripes * a.n_segs;
+  if (!EXT && resident > 0)
+    warps = plain_layout<K, CPL>(a, resident, g_cfg.gen_cost > 0.f ? g_cfg.gen_cost : (CPL == 4 ? 4.0f : 2.5f));
   if (EXT) {
     a.ext.nc = a.ext.nr = 0;
     const int np = a.ext.tfsf_npml;

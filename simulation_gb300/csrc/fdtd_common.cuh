@@ -55,6 +55,27 @@ __device__ __forceinline__ void h_update_pml(float ez, float ez_jp1, float ez_ip
   hy = __fmaf_rn(fx3, hy, -__fmul_rn(fx2, __fmaf_rn(fy1, ihy, __fmul_rn(0.5f, cy))));
 }
 
+// The same two updates where every PML coefficient of the cell is the unit
+// profile (gx2 = gx3 = gy2 = gy3 = 1, fx1 = fy1 = 0, fx2 = fx3 = fy2 = fy3 = 1,
+// i.e. outside the absorbing layer).  The general formulas then reduce
+// exactly: gx3*gy3 = 1 and gx2*gy2*0.5 = 0.5 are exact, fma(1, a, b) rounds
+// a + b once, and fma(0, ihx, y) = y for finite ihx (up to the sign of a
+// zero).  So these return the same values as d_update / h_update_pml called
+// with the unit coefficients, with 2 and 6 fewer operations per cell.
+__device__ __forceinline__ float d_update_unit(float dz, float hy, float hy_im1, float hx, float hx_jm1) {
+  const float curl = __fadd_rn(__fsub_rn(__fsub_rn(hy, hy_im1), hx), hx_jm1);
+  return __fadd_rn(dz, __fmul_rn(0.5f, curl));
+}
+__device__ __forceinline__ void h_update_pml_unit(float ez, float ez_jp1, float ez_ip1, float& hx, float& hy,
+                                                  float& ihx, float& ihy) {
+  const float cx = __fsub_rn(ez, ez_jp1);
+  const float cy = __fsub_rn(ez, ez_ip1);
+  ihx = __fadd_rn(ihx, cx);
+  ihy = __fadd_rn(ihy, cy);
+  hx = __fadd_rn(hx, __fmul_rn(0.5f, cx));
+  hy = __fsub_rn(hy, __fmul_rn(0.5f, cy));
+}
+
 // Hx/Hy update without PML, fd2d/python/fd2d_3_1.py:70-71:
 //   hx += 0.5*(ez[i,j]-ez[i,j+1]);  hy -= 0.5*(ez[i,j]-ez[i+1,j])
 __device__ __forceinline__ void h_update_free(float ez, float ez_jp1, float ez_ip1, float& hx, float& hy) {

@@ -168,6 +168,26 @@ class Sim1D:
         if v:
             raise _lib.FdtdError(_lib.lib().fdtd_status_to_error(v), f"Sim1D status word {v:#x}")
 
+    def amplitude_phase(self, probe: int = 0):
+        """(amp, phase) float64 [nf][nx] of the full-field DFT against probe
+        ``probe`` as input (fd1d/program/fd1d_2_2.py:145-146, on the device)."""
+        if self.r_pt is None:
+            raise ValueError("amplitude_phase needs freq=... and full_dft=True")
+        if not 0 <= probe < len(self.probes):
+            raise ValueError("no such probe")
+        from .output import amplitude_phase
+        return amplitude_phase(self.r_pt, self.i_pt, self.r_pr[probe], self.i_pr[probe])
+
+    def head(self, name: str = "ex", n: int = 50) -> str:
+        """``print(ex[0:50])`` of the reference's benchmark twins (fd1d/program/test_1_3.py:70)."""
+        from .output import head
+        return head(getattr(self, name), n)
+
+    def save(self, path: str, names=None) -> str:
+        """Write the fields to an .npz archive (or .npy files in a directory)."""
+        from .output import save
+        return save(self, path, names)
+
     FIELDS = ("ex", "hy", "dx", "ix", "sx", "bc", "r_pt", "i_pt", "r_pr", "i_pr")
 
     def state_dict(self) -> dict:

@@ -48,6 +48,26 @@ def pml_profiles(nx: int, ny: int, npml: int, grade: float = 0.33) -> dict:
     return v
 
 
+def pml_cells(pml: pmlayer | None) -> int:
+    """Thickness in cells of the absorbing layer a ``pmlayer`` holds (0 for
+    none): the longest run of non-unit coefficients at either end of the ten
+    vectors.  Read once from the device when a program is set up; the fused
+    kernel uses it only to balance its work."""
+    if pml is None:
+        return 0
+    unit = dict(fx1=0.0, fy1=0.0)
+    n = 0
+    for k in pmlayer._fields:
+        v = getattr(pml, k).detach().cpu().numpy()
+        bad = np.flatnonzero(v != unit.get(k, 1.0))
+        lo, hi = bad[bad < v.size // 2], bad[bad >= v.size // 2]
+        if lo.size:
+            n = max(n, int(lo.max()) + 1)
+        if hi.size:
+            n = max(n, int(v.size - hi.min()))
+    return n
+
+
 def pmlparam(nx: int, ny: int, npml: int, grade: float = 0.33, device="cuda") -> pmlayer:
     """``pmlayer`` of float32 device vectors (npml=0: no absorbing layer)."""
     v = pml_profiles(nx, ny, npml, grade)
@@ -90,6 +110,7 @@ class SimTM2D:
         self.dt = dt
         self.lossy = lossy
         self.pml = pml
+        self.pml_cells = pml_cells(pml)
         self.source = source
         self.tfsf_npml = tfsf_npml
         self.freq = None if freq is None else np.asarray(freq, dtype=np.float64).reshape(-1)
@@ -143,6 +164,7 @@ class SimTM2D:
         if self.pml is not None:
             for k in pmlayer._fields:
                 setattr(p.pml, k, ptr(getattr(self.pml, k)))
+            p.pml_cells = self.pml_cells
         p.naz = ptr(self.naz)
         p.nbz = ptr(self.nbz)
         if self.source is not None:
@@ -252,6 +274,32 @@ class SimTM2D:
         if v:
             rc = _lib.lib().fdtd_status_to_error(v)
             raise _lib.FdtdError(rc, f"SimTM2D status word {v:#x} at t={self.t}")
+
+    def amplitude_phase(self, row: int | None = None, j0: int | None = None, j1: int | None = None):
+        """(amp, phase) float64 [nf][j1-j0+1] along one row of the DFT against
+        the incident line's input (fd2d/python/fd2d_3_4.py:280-284: row
+        nx//2-1, columns npml-1 .. ny-npml with npml the TF/SF boundary)."""
+        if self.r_pt is None or self.r_in is None:
+            raise ValueError("amplitude_phase needs freq=... and tfsf_npml > 0 (the input is ezi[6])")
+        npml = self.tfsf_npml
+        row = self.nx // 2 - 1 if row is None else row
+        j0 = npml - 1 if j0 is None else j0
+        j1 = self.ny - npml if j1 is None else j1
+        if not (0 <= row < self.nx and 0 <= j0 <= j1 < self.ny):
+            raise ValueError("row/columns outside the grid")
+        from .output import amplitude_phase
+        return amplitude_phase(self.r_pt, self.i_pt, self.r_in, self.i_in, row * self.ny + j0, j1 - j0 + 1)
+
+    def head(self, name: str = "ez", row: int = 2, n: int = 50) -> str:
+        """``print(ez[2][0:50])`` of the reference's benchmark twins
+        (fd2d/python/test_3_4.py:292): the first ``n`` values of one row."""
+        from .output import head
+        return head(getattr(self, name)[row], n)
+
+    def save(self, path: str, names=None) -> str:
+        """Write the fields to an .npz archive (or .npy files in a directory)."""
+        from .output import save
+        return save(self, path, names)
 
     FIELDS = ("dz", "ez", "iz", "hx", "hy", "ihx", "ihy", "ezi", "hxi", "bc", "r_pt", "i_pt", "r_in", "i_in")
 

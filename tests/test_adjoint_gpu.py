@@ -96,3 +96,91 @@ def test_adjoint_vs_central_fd_config4(cuda_lib):
     rl2 = float(np.linalg.norm(err) / np.linalg.norm(ref))
     print(f"central FD vs adjoint on 32 cells: rel-L2 {rl2:.3e}, worst {err.max():.3e} of max |fd| {ref.max():.3e}")
     assert rl2 <= 1e-3, f"rel-L2 {rl2:.3e}"
+
+
+def _stepwise_gradient(pr):
+    """dJ/dnaz by the reference-granularity entry points: the forward as
+    fdtd2d_step_n calls per checkpoint segment, each segment's states
+    recomputed with one-step fdtd2d_pass calls, then fdtd2d_adjoint_step
+    (two kernels, in place) once per step."""
+    import ctypes as C
+    from simulation_gb300 import _lib
+    lib = _lib.lib()
+    s, p = pr.sim, pr.sim._p
+    nx, ny, ns, cp = pr.nx, pr.ny, pr.ns, pr.cp
+    names = ("dz", "iz", "hx", "hy", "ihx", "ihy")
+    z = lambda *sh: torch.zeros(sh, dtype=torch.float32, device="cuda")  # noqa: E731
+
+    def fields(buf):
+        f = _lib.Fields2D()
+        for k, name in enumerate(names):
+            setattr(f, name, buf[k].data_ptr())
+        return f
+
+    s.reset()
+    trace = z(ns)
+    p.probe_i, p.probe_j, p.probe_len = pr.probe[0], pr.probe[1], ns
+    s._s.probe_ez = trace.data_ptr()
+    ncp = -(-ns // cp)
+    ckpt = z(ncp, 6, nx, ny)
+    for c in range(ncp):
+        for k, name in enumerate(names):
+            ckpt[c, k].copy_(getattr(s, name))
+        s.step(min(cp, ns - c * cp))
+    s._s.probe_ez = None
+    seg, adj, tmp, ez = z(cp, 6, nx, ny), z(6, nx, ny), z(nx, ny), z(nx, ny)
+    grad = z(pr.box[2], pr.box[3])
+    box = _lib.Box2D(*pr.box)
+    st = _lib.stream_ptr()
+    for c in reversed(range(ncp)):
+        t0, L = c * cp, min(cp, ns - c * cp)
+        seg[0].copy_(ckpt[c])
+        for k in range(1, L):
+            assert lib.fdtd2d_pass(C.byref(p), C.byref(fields(seg[k - 1])), C.byref(fields(seg[k])), ez.data_ptr(),
+                                   t0 + k - 1, 1, None, st) == 0
+        for t in range(t0 + L, t0, -1):
+            assert lib.fdtd2d_adjoint_step(t, C.byref(p), C.byref(fields(seg[t - t0 - 1])), C.byref(fields(adj)),
+                                           tmp.data_ptr(), pr.probe[0], pr.probe[1], 2.0, box, grad.data_ptr(),
+                                           None, st) == 0
+    torch.cuda.synchronize()
+    return float((trace.double() ** 2).sum()), trace, grad
+
+
+@pytest.mark.parametrize("sigma,cp", [(0.0, 16), (0.05, 21), (0.05, 64)])
+def test_one_call_adjoint_equals_stepwise(cuda_lib, sigma, cp):
+    """fdtd2d_tm_adjoint_forward/_reverse (recording passes, fused reverse
+    kernel, overlapped streams) give the probe trace and dJ/dnaz bit for bit
+    equal to the step-by-step entry points; J (summed in double on the
+    device) agrees to rounding."""
+    pr, eps = _small(cp=cp, sigma=sigma)
+    pr.use_graphs = False
+    pr.set_eps(eps)
+    J = pr.forward()
+    g = pr.gradient_naz().clone()
+    trace = pr.trace.clone()
+    J2, trace2, g2 = _stepwise_gradient(pr)
+    assert torch.equal(trace, trace2)
+    assert abs(J - J2) <= 1e-12 * abs(J2)
+    assert torch.equal(g, g2)
+    assert float(g.abs().max()) > 0
+
+
+def test_one_call_adjoint_single_entry(cuda_lib):
+    """fdtd2d_tm_adjoint (forward and reverse in one call) equals the split calls."""
+    import ctypes as C
+    from simulation_gb300 import _lib
+    pr, eps = _small(cp=16, sigma=0.05)
+    pr.use_graphs = False
+    pr.set_eps(eps)
+    J = pr.forward()
+    g = pr.gradient_naz().clone()
+    trace = torch.zeros_like(pr.trace)
+    Jd = torch.zeros(1, dtype=torch.float64, device="cuda")
+    g1 = torch.zeros_like(g)
+    gn = torch.zeros_like(g)
+    _lib.call("fdtd2d_tm_adjoint", C.byref(pr.sim._p), C.byref(pr.ap), trace.data_ptr(), Jd.data_ptr(),
+              g1.data_ptr(), gn.data_ptr(), pr.ws.data_ptr(), pr.ws.numel(), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    assert float(Jd.item()) == J
+    assert torch.equal(g1, g)
+    assert float(gn.abs().max()) > 0  # dJ/dnbz over the lossy box

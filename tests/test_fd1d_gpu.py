@@ -37,10 +37,15 @@ def test_program_vs_golden(cuda_lib, golden, name):
         if x is not None:
             assert torch.equal(x, y), f"{name}: fused vs per-function {k}"
     if f"{name}_amp2" in g:
+        # the reference's post-processing (fd1d/program/fd1d_2_2.py:145-146) on the device
+        amp, phase = a.amplitude_phase()
         rp, ip = _np(a.r_pt), _np(a.i_pt)
         rin, iin = _np(a.r_pr)[0][:, None], _np(a.i_pr)[0][:, None]
-        amp = 1 / np.hypot(rin, iin) * np.hypot(rp, ip)
-        assert_parity(amp[2], g[f"{name}_amp2"], tol=1e-4, what=f"{name} amplitude")
+        np.testing.assert_allclose(amp.cpu().numpy(), 1 / np.hypot(rin, iin) * np.hypot(rp, ip), rtol=1e-14)
+        np.testing.assert_allclose(phase.cpu().numpy(), np.arctan2(ip, rp) - np.arctan2(iin, rin), rtol=0,
+                                   atol=1e-13)
+        err = assert_parity(amp[2].cpu().numpy(), g[f"{name}_amp2"], tol=1e-5, what=f"{name} amplitude")
+        print(f"\n{name} amplitude vs golden: max/peak {err[0]:.2e} relL2 {err[1]:.2e}")
 
 
 def test_config1_vs_oracle(cuda_lib):
