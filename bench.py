@@ -49,9 +49,9 @@ WORKLOAD = ("2D TM PML lossy-cylinder benchmark program: 8192x8192, npml=32 grad
             "cylinder r=1000 eps_r=30 sigma=0.3, hard Gaussian Dz source t0=20 spread=6, 2000 steps, FP32")
 # DRAM bytes per cell per fused K=4 pass, from one ncu capture of the fused kernel
 # on the 4096^2 case ((dram__bytes_read.sum + dram__bytes_write.sum) / cells =
-# 1005.3 MB / 16.78 M cells, profiles/k_march_K4_CPL2_full_4096.md); traffic
+# 1009.4 MB / 16.78 M cells, profiles/k_march_K4_CPL4_full_4096.md); traffic
 # grows in proportion to the cells, so it is scaled to the launch size
-NCU_TRAFFIC_BYTES_PER_CELL_PASS = {4: 59.9}
+NCU_TRAFFIC_BYTES_PER_CELL_PASS = {4: 60.2}
 
 
 def _peaks():
@@ -148,14 +148,30 @@ def _cpu_setup(nx: int, ny: int):
     return _CPU_SETUP[key]
 
 
-def cpu_port_rate(nx: int, ny: int, steps: int, threads: int | None = None) -> dict:
-    """Time the float32 OpenMP C port of the reference loops on this host."""
+def host_cpu() -> str:
+    """The host CPU's model as lscpu reports it (with its core count)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        d = dict(line.split(":", 1) for line in out.splitlines() if ":" in line)
+        name = (d.get("Model name") or d.get("Vendor ID") or "unknown").strip()
+        return f"{name}, {os.cpu_count()} logical CPUs, {(d.get('Architecture') or '').strip()}"
+    except Exception:
+        return f"unknown, {os.cpu_count()} logical CPUs"
+
+
+def cpu_port_rate(nx: int, ny: int, steps: int, threads: int | None = None, native: bool = False) -> dict:
+    """Time the float32 OpenMP C port of the reference loops on this host:
+    the portable -O3 build, or (native) the build tuned for this host's CPU."""
     import numpy as np
 
     from oracle import ccore
-    lib = ccore.lib32()
+    lib = ccore.lib32_native() if native else ccore.lib32()
+    if lib is None:
+        return {"value": 0.0, "seconds": 0.0, "cores": 0, "sample": "native build unavailable"}
     if threads:
         lib.oracle_set_threads(threads)
+    else:
+        lib.oracle_set_threads(os.cpu_count() or 1)
     nth = lib.oracle_threads()
     pd, naz, nbz = _cpu_setup(nx, ny)
     f = {k: np.zeros((nx, ny), dtype=np.float32) for k in ("dz", "ez", "iz", "hx", "hy", "ihx", "ihy")}
@@ -164,8 +180,21 @@ def cpu_port_rate(nx: int, ny: int, steps: int, threads: int | None = None) -> d
     t0 = time.perf_counter()
     ccore.fd2d_steps(lib, np.float32, nx, ny, 1, steps, pd, naz, nbz, (1, nx // 2, ny // 2), table, f)
     el = time.perf_counter() - t0
-    return {"value": nx * ny * steps / el / 1e9, "seconds": el, "cores": nth,
+    flags = "-O3 -march/-mcpu=native" if native else "-O3"
+    return {"value": nx * ny * steps / el / 1e9, "seconds": el, "cores": nth, "build": f"gcc {flags} -fopenmp",
             "sample": f"{nx}x{ny} grid, {steps} steps of the same lossy PML update (float32 C port, OpenMP)"}
+
+
+def cpu_best_rate(nx: int, ny: int, steps: int, threads: int | None = None) -> dict:
+    """The faster of the portable and the host-tuned builds of the float32
+    port (the other one's rate is kept beside it), with the host CPU named."""
+    a = cpu_port_rate(nx, ny, steps, threads)
+    b = cpu_port_rate(nx, ny, steps, threads, native=True)
+    best, other = (b, a) if b["value"] > a["value"] else (a, b)
+    best = dict(best)
+    best["other_build"] = {"build": other.get("build"), "value": other["value"]}
+    best["cpu"] = host_cpu()
+    return best
 
 
 def max_over_ranks(ms: float, world: int, device) -> float:
@@ -209,9 +238,11 @@ def run_reference(args) -> None:
     steps_per_sample = int(os.environ.get("FDTD_REF_SAMPLE_STEPS", "20"))
     for _ in range(args.warmup):
         cpu_port_rate(NX, NY, 1)
+    # the faster of the two builds on this host, then the timed samples with it
+    native = cpu_port_rate(NX, NY, 2, native=True)["value"] > cpu_port_rate(NX, NY, 2)["value"]
     vals = []
     for _ in range(args.steps):
-        r = cpu_port_rate(NX, NY, steps_per_sample)
+        r = cpu_port_rate(NX, NY, steps_per_sample, native=native)
         vals.append(r)
     tot_cells = sum(NX * NY * steps_per_sample for _ in vals)
     tot_s = sum(v["seconds"] for v in vals)
@@ -222,7 +253,7 @@ def run_reference(args) -> None:
             "data": "synthetic (deterministic benchmark program, no RNG)",
             "config": {"workload": WORKLOAD, "sample_steps_per_step": steps_per_sample, "grid": [NX, NY]},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"]},
+                             "sample": vals[0]["sample"], "build": vals[0]["build"], "cpu": host_cpu()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -304,11 +335,12 @@ def run_ours(args) -> None:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS", "150")))
+        cpu = cpu_best_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS", "150")))
         cpu["unit"] = UNIT
         cpu["kind"] = "port"
-        one = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS_1T", "10")), threads=1)
-        cpu["single_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"]}
+        one = cpu_port_rate(NX, NY, int(os.environ.get("FDTD_CPU_SAMPLE_STEPS_1T", "10")), threads=1,
+                            native=cpu["build"] != "gcc -O3 -fopenmp")
+        cpu["single_thread"] = {"value": one["value"], "cores": 1, "sample": one["sample"], "build": one["build"]}
         try:
             cpu["numpy_reference_form"] = numpy_reference_rate()
         except Exception as exc:  # reported, never fatal to the bench line
@@ -461,14 +493,23 @@ def _cpu_batch1d(batch, runner, nsample: int = 64) -> dict:
     b = batch.subset(idx)
     lca, lcb = B.layer_coeffs(b.epsr, b.sigma)
     ns = runner.nsteps
-    lib = ccore.lib32()
-    t0 = time.perf_counter()
-    ccore.fd1d_batch(lib, np.float32, b.ke, b.layer_off, b.layer_start, b.layer_end, lca, lcb, b.src_k,
-                     runner.src_table.double().cpu().numpy()[:ns], ns, runner.dft_cos.double().cpu().numpy()[:ns],
-                     runner.dft_sin.double().cpu().numpy()[:ns], b.probe_in, b.probe_out)
-    el = time.perf_counter() - t0
+    tab = runner.src_table.double().cpu().numpy()[:ns]
+    dc, ds = runner.dft_cos.double().cpu().numpy()[:ns], runner.dft_sin.double().cpu().numpy()[:ns]
+    best = None
+    # the faster of the portable and the host-tuned builds
+    for lib, build in ((ccore.lib32(), "gcc -O3 -fopenmp"), (ccore.lib32_native(), "gcc -O3 -march/-mcpu=native -fopenmp")):
+        if lib is None:
+            continue
+        lib.oracle_set_threads(os.cpu_count() or 1)
+        t0 = time.perf_counter()
+        ccore.fd1d_batch(lib, np.float32, b.ke, b.layer_off, b.layer_start, b.layer_end, lca, lcb, b.src_k, tab, ns,
+                         dc, ds, b.probe_in, b.probe_out)
+        el = time.perf_counter() - t0
+        if best is None or el < best[0]:
+            best = (el, build, int(lib.oracle_threads()))
+    el, build, cores = best
     return {"Gcell_updates_per_s": float(b.ke.sum()) * ns / el / 1e9, "spectra_per_s": b.nruns / el,
-            "cores": int(lib.oracle_threads()), "kind": "port",
+            "cores": cores, "kind": "port", "build": build,
             "sample": f"{b.nruns} runs of the batch, {ns} steps (float32 C port, OpenMP over runs)"}
 
 

@@ -194,9 +194,14 @@ int fdtd2d_set_march_balance(float gen_cost);
  * No counterpart in the reference.  The ping-pong workspace is a static device
  * array of FDTD2D_NOALLOC_SCRATCH_BYTES inside this library, held by every GPU
  * that loads it until the process exits; grids needing more (more than
- * FDTD2D_NOALLOC_MAX_CELLS cells) get FDTD_ERR_SIZE.  Allocates nothing.  The
- * first call on a device looks the array's address up (cudaGetSymbolAddress):
- * make it before any stream capture.  All calls share the array (it keeps the
+ * FDTD2D_NOALLOC_MAX_CELLS cells) get FDTD_ERR_SIZE.  Allocates nothing itself.
+ * The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress): with lazy module loading (the CUDA default) that is
+ * when the driver reserves the array, so that first call can fail with
+ * FDTD_ERR_CUDA if the device is out of memory; make it up front, before any
+ * stream capture and before a memory budget is locked.  The address is kept
+ * for the life of the process: calls after a cudaDeviceReset are not
+ * supported.  All calls share the array (it keeps the
  * last call's contents, none of which must start at zero); calls that overlap
  * on the GPU race on it.  With TF/SF or the DFT on and a workspace larger than
  * the array, each step is one fdtd2d_step_n call of one step instead. */

@@ -1,7 +1,8 @@
 """ctypes access to the C oracle (test infrastructure only).
 
 ``lib64()`` is the float64 restatement (bit-identical to the NumPy oracle),
-``lib32()`` the float32 OpenMP build used as the timed CPU baseline.
+``lib32()`` the float32 OpenMP build and ``lib32_native()`` the same built for
+the host's CPU: the timed CPU baseline.
 ``ref(name)`` loads a reference C program compiled from its own sources
 (``make -C oracle ref``), when that was possible.
 """
@@ -50,6 +51,16 @@ def lib64():
 
 def lib32():
     return _load("liboracle32.so")
+
+
+def lib32_native():
+    """The float32 port built for this host's CPU (-march/-mcpu=native), or
+    None where the compiler could not build it.  Timing only."""
+    if not os.path.exists(os.path.join(HERE, "_build", "liboracle32n.so")):
+        build()
+    if not os.path.exists(os.path.join(HERE, "_build", "liboracle32n.so")):
+        return None
+    return _load("liboracle32n.so")
 
 
 def _p(a):

@@ -18,11 +18,14 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("FDTD_REFERENCE_ROOT", "/root/reference")
+# the checkout's root comes from the environment (tests/golden/make_golden.py
+# sets it); unset means no reference here
+REF_ROOT = os.environ.get("FDTD_REFERENCE_ROOT", "")
 
 
 def available() -> bool:
-    return os.path.isdir(os.path.join(REF_ROOT, "fd1d")) and os.path.isdir(os.path.join(REF_ROOT, "fd2d"))
+    return bool(REF_ROOT) and os.path.isdir(os.path.join(REF_ROOT, "fd1d")) and \
+        os.path.isdir(os.path.join(REF_ROOT, "fd2d"))
 
 
 class _Anything:

@@ -51,18 +51,18 @@ __device__ __forceinline__ float lam_cx(const AdjArgs& a, int i, int j) {
   // adjoint of cx at (i, j) from hx', ihx' there (0 where H is not applied)
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
   const size_t n = (size_t)i * a.ny + j;
-  const float lhx = a.adj.hx[n];
+  const float lhx = __ldg(a.adj.hx + n);
   const float fy2 = __ldg(a.pml.fy2 + j);
-  const float lihx_t = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, a.adj.ihx[n]);
+  const float lihx_t = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, __ldg(a.adj.ihx + n));
   return __fmaf_rn(__fmul_rn(0.5f, fy2), lhx, lihx_t);
 }
 
 __device__ __forceinline__ float lam_cy(const AdjArgs& a, int i, int j) {
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
   const size_t n = (size_t)i * a.ny + j;
-  const float lhy = a.adj.hy[n];
+  const float lhy = __ldg(a.adj.hy + n);
   const float fx2 = __ldg(a.pml.fx2 + i);
-  const float lihy_t = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, a.adj.ihy[n]);
+  const float lihy_t = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, __ldg(a.adj.ihy + n));
   return __fmaf_rn(-__fmul_rn(0.5f, fx2), lhy, lihy_t);
 }
 
@@ -75,15 +75,16 @@ __device__ __forceinline__ float lam_cy(const AdjArgs& a, int i, int j) {
 __device__ __forceinline__ float adj_e(const AdjArgs& a, int i, int j, bool own) {
   const size_t n = (size_t)i * a.ny + j;
   // forward recompute of dz' and ez at this cell (same formulas as the forward)
-  float dzp = a.fwd.dz[n];
+  float dzp = __ldg(a.fwd.dz + n);
   if (i >= 1 && j >= 1)
-    dzp = d_update(dzp, a.fwd.hy[n], a.fwd.hy[n - a.ny], a.fwd.hx[n], a.fwd.hx[n - 1], __ldg(a.pml.gx3 + i),
+    dzp = d_update(dzp, __ldg(a.fwd.hy + n), __ldg(a.fwd.hy + n - a.ny), __ldg(a.fwd.hx + n),
+                   __ldg(a.fwd.hx + n - 1), __ldg(a.pml.gx3 + i),
                    __ldg(a.pml.gy3 + j), __ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j));
   if (a.src_kind != FDTD_SRC_NONE && i == a.src_i && j == a.src_j) {
     const float v = __ldg(a.src_table + a.t - 1);
     dzp = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(dzp, v);
   }
-  const float izv = a.nbz ? a.fwd.iz[n] : 0.f;
+  const float izv = a.nbz ? __ldg(a.fwd.iz + n) : 0.f;
   const float diff = __fsub_rn(dzp, izv);
   const float naz = __ldg(a.naz + n);
   const float ez = __fmul_rn(naz, diff);
@@ -92,7 +93,7 @@ __device__ __forceinline__ float adj_e(const AdjArgs& a, int i, int j, bool own)
   if (i == a.probe_i && j == a.probe_j) lez = __fmaf_rn(a.probe_w, ez, lez);
   // E backward
   const float nbz = a.nbz ? __ldg(a.nbz + n) : 0.f;
-  const float liz = a.nbz ? a.adj.iz[n] : 0.f;
+  const float liz = a.nbz ? __ldg(a.adj.iz + n) : 0.f;
   const float lezt = __fmaf_rn(nbz, liz, lez);
   if (own) {
     if (a.nbz) a.out.iz[n] = __fmaf_rn(-naz, lezt, liz);
@@ -103,7 +104,7 @@ __device__ __forceinline__ float adj_e(const AdjArgs& a, int i, int j, bool own)
       if (a.grad_nbz) a.grad_nbz[b] = __fmaf_rn(liz, ez, a.grad_nbz[b]);
     }
   }
-  return __fmaf_rn(naz, lezt, a.adj.dz[n]);
+  return __fmaf_rn(naz, lezt, __ldg(a.adj.dz + n));
 }
 
 // cb*T at (i, j): the D adjoint flowing into the curl's H terms (0 where D is
@@ -127,7 +128,8 @@ __device__ __forceinline__ void adj_dh(const AdjArgs& a, int i, int j, float T, 
   else ldz = T;
   const float dg = dgrad(a, i, j, T);
   const bool hm = (i <= a.nx - 2) && (j <= a.ny - 2);
-  float lhx = a.adj.hx[n], lhy = a.adj.hy[n], lihx = a.adj.ihx[n], lihy = a.adj.ihy[n];
+  float lhx = __ldg(a.adj.hx + n), lhy = __ldg(a.adj.hy + n), lihx = __ldg(a.adj.ihx + n),
+        lihy = __ldg(a.adj.ihy + n);
   if (hm) {
     const float fy2 = __ldg(a.pml.fy2 + j), fx2 = __ldg(a.pml.fx2 + i);
     lihx = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, lihx);
@@ -162,28 +164,42 @@ __global__ void k_adj_b(const AdjArgs a) {
   adj_dh(a, i, j, a.tmp[n], Ti, Tj);
 }
 
-// Fused form: one block takes a TI x TJ tile, computes T on the tile plus
-// one row and one column of halo into shared memory, then runs the D/H part
-// for the tile.  It reads the adjoints after step t (a.adj) and writes those
-// before it to other arrays (a.out): a halo cell's inputs belong to the
-// neighbouring tile, which must not have overwritten them.  Same per-cell
-// arithmetic as the two-kernel form, so the results are bitwise equal.
-constexpr int kAdjTJ = 32, kAdjTI = 8;
-__global__ void __launch_bounds__(kAdjTJ * kAdjTI) k_adj_fused(const AdjArgs a) {
+// Fused form: one block of 32 x 8 threads takes a kAdjTI x 32 tile (each
+// thread kAdjTI/8 rows), computes T on the tile plus one row and one column
+// of halo into shared memory (warps 0 and 1 and one lane of warp 2 take the
+// halo), then runs the D/H part for the tile.  It reads the adjoints after
+// step t (a.adj) and writes those before it to other arrays (a.out): a halo
+// cell's inputs belong to the neighbouring tile, which must not have
+// overwritten them.  Same per-cell arithmetic as the two-kernel form, so the
+// results are bitwise equal.
+constexpr int kAdjTJ = 32, kAdjTI = 16, kAdjThreadsY = 8, kAdjRows = kAdjTI / kAdjThreadsY;
+__global__ void __launch_bounds__(kAdjTJ * kAdjThreadsY) k_adj_fused(const AdjArgs a) {
   __shared__ float sT[kAdjTI + 1][kAdjTJ + 1];
   const int j0 = blockIdx.x * kAdjTJ, i0 = blockIdx.y * kAdjTI;
-  const int tid = threadIdx.y * kAdjTJ + threadIdx.x;
-  for (int idx = tid; idx < (kAdjTI + 1) * (kAdjTJ + 1); idx += kAdjTI * kAdjTJ) {
-    const int li = idx / (kAdjTJ + 1), lj = idx - li * (kAdjTJ + 1);
-    const int i = i0 + li, j = j0 + lj;
-    float T = 0.f;
-    if (i < a.nx && j < a.ny) T = adj_e(a, i, j, li < kAdjTI && lj < kAdjTJ);
-    sT[li][lj] = T;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int j = j0 + tx;
+#pragma unroll
+  for (int k = 0; k < kAdjRows; ++k) {
+    const int li = ty + kAdjThreadsY * k, i = i0 + li;
+    sT[li][tx] = (i < a.nx && j < a.ny) ? adj_e(a, i, j, true) : 0.f;
+  }
+  if (ty == 0) {  // halo row below the tile
+    const int i = i0 + kAdjTI;
+    sT[kAdjTI][tx] = (i < a.nx && j < a.ny) ? adj_e(a, i, j, false) : 0.f;
+  } else if (ty == 1 && tx < kAdjTI) {  // halo column right of the tile
+    const int i = i0 + tx, jj = j0 + kAdjTJ;
+    sT[tx][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, i, jj, false) : 0.f;
+  } else if (ty == 2 && tx == 0) {  // and their corner
+    const int i = i0 + kAdjTI, jj = j0 + kAdjTJ;
+    sT[kAdjTI][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, i, jj, false) : 0.f;
   }
   __syncthreads();
-  const int i = i0 + threadIdx.y, j = j0 + threadIdx.x;
-  if (i >= a.nx || j >= a.ny) return;
-  adj_dh(a, i, j, sT[threadIdx.y][threadIdx.x], sT[threadIdx.y + 1][threadIdx.x], sT[threadIdx.y][threadIdx.x + 1]);
+  if (j >= a.ny) return;
+#pragma unroll
+  for (int k = 0; k < kAdjRows; ++k) {
+    const int li = ty + kAdjThreadsY * k, i = i0 + li;
+    if (i < a.nx) adj_dh(a, i, j, sT[li][tx], sT[li + 1][tx], sT[li][tx + 1]);
+  }
 }
 
 }  // namespace
@@ -214,7 +230,7 @@ int launch_adjoint_fused(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd
   a.box = box;
   a.grad_naz = grad_naz;
   a.grad_nbz = grad_nbz;
-  const dim3 blk(kAdjTJ, kAdjTI);
+  const dim3 blk(kAdjTJ, kAdjThreadsY);
   const dim3 grd((p.ny + kAdjTJ - 1) / kAdjTJ, (p.nx + kAdjTI - 1) / kAdjTI);
   k_adj_fused<<<grd, blk, 0, st>>>(a);
   return fdtd_host::check_launch();

@@ -56,12 +56,6 @@ struct MarchExt {
   const float* dft_cos;  // [t-1][nf] tables of the whole run
   const float* dft_sin;
   float *r_pt, *i_pt;  // [nf][nx][ny] accumulators
-  // Set by the launcher: segments that reach a TF/SF edge run as two halves
-  // (their warps carry the slower edge logic).  They are the edge stripes
-  // tf_c[0..nc) with every segment, and the other stripes with the edge
-  // segments tf_r[0..nr); both lists ascending.  nc = nr = 0: no halving.
-  int nc, nr;
-  int tf_c[6], tf_r[6];
 };
 constexpr int kMarchMaxNf = 8;         // DFT frequencies the fused pass carries
 constexpr int kLineMaxNy = 16384;      // incident line held in shared memory

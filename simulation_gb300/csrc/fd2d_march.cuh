@@ -264,9 +264,9 @@ __device__ __forceinline__ void pf_dft(const MarchArgs& a, float* rg, int row, i
 // reads it at run time) and the ring is updated for every row and lane, with
 // zero-filled copies and predicated stores where the warp does not own the
 // cell.  Branches there cost the EXT kernel 40% at 2048^2.  The edge logic
-// itself is compiled only into the body that warps touching a TF/SF edge run
-// (TF = true: a stripe with an edge column, or rows reaching an edge row);
-// the others run the body without it.
+// is compiled into the general form of the iteration only (TF = true when
+// the TF/SF source is on): the interior form runs away from the box's edge
+// rows and outside the stripes that hold its edge columns.
 // One row iteration of a warp's march, in two forms sharing the same register
 // state:
 //   * the general form (GEN) handles every case: PML coefficients per row and
@@ -349,7 +349,18 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe,
   }
   const bool src_here = a.src_kind != FDTD_SRC_NONE && a.src_j >= jw0 && a.src_j < jw0 + W;
   const bool probe_here = PROBE && a.probe_j >= jw0 && a.probe_j < jw0 + W;
-  const bool cint = !TFS && __all_sync(FULL, col_ok);
+  // TF/SF: the box's edge columns (inctdz at np-1 and ny-np, incthx at np-2
+  // and ny-np, for rows np-1 .. nx-np) make a stripe general; the edge rows
+  // np-2 and nx-np (incthy) are bad rows for every stripe (row_ok)
+  const int np_edge = TFS ? a.ext.tfsf_npml : 0;
+  if (np_edge > 0) {
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int j = j0 + c;
+      col_ok &= j != np_edge - 2 && j != np_edge - 1 && j != ny - np_edge;
+    }
+  }
+  const bool cint = __all_sync(FULL, col_ok);
   if constexpr (DFT) {
     for (int x = lane; x < K * nf; x += 32) {
       const int s = x / nf, f = x - s * nf;
@@ -385,6 +396,7 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe,
           __ldg(a.pml.fx2 + row) == 1.f && __ldg(a.pml.fx3 + row) == 1.f;
     if (src_here && row == a.src_i) g = false;
     if (probe_here && row == a.probe_i) g = false;
+    if (np_edge > 0 && (row == np_edge - 2 || row == nx - np_edge)) g = false;
     return __ballot_sync(FULL, g);
   };
 
@@ -694,24 +706,6 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe,
   if (a.check_finite && __any_sync(FULL, !finite_ok) && lane == 0) raise_status(a.status, ST_NONFINITE);
 }
 
-// TF/SF edges a warp's work can reach (np = tfsf_npml > 0): a column np-2,
-// np-1 or ny-np among its stripe's columns (halo included), or a row np-2 or
-// nx-np (hy edges) among the rows its levels update (segment rows widened by
-// the 2K-row cone and the K-row lag).  The launcher builds the halving lists
-// from the same two tests.
-template <int CPL>
-__host__ __device__ inline bool tf_stripe(int np, int ny, int stripe) {
-  constexpr int OUTW = 32 * CPL - 2 * HALO;
-  const int c0 = stripe * OUTW - HALO, c1 = c0 + 32 * CPL - 1;
-  return (np - 2 >= c0 && np - 2 <= c1) || (np - 1 >= c0 && np - 1 <= c1) || (ny - np >= c0 && ny - np <= c1);
-}
-template <int K>
-__host__ __device__ inline bool tf_segment(int np, int nx, int seg_rows, int seg) {
-  const int i_s = seg * seg_rows;
-  const int r0 = i_s - 2 * K, r1 = (i_s + seg_rows < nx ? i_s + seg_rows : nx) + K;
-  return (np - 2 >= r0 && np - 2 <= r1) || (nx - np >= r0 && nx - np <= r1);
-}
-
 // Warp -> work of the plain kernels (layout: plain_layout): warps
 // 0 .. n_int*n_segs-1 take the stripes away from the edges, the rest the
 // general stripes at either edge with their shorter segments.  False: no work.
@@ -737,71 +731,40 @@ __host__ __device__ inline bool plain_work(const MarchArgs& a, int gw, int& stri
   return i_s < i_e;
 }
 
-__device__ __forceinline__ int pick6(const int (&v)[6], int i) {  // v[i] without a local-memory copy
-  return i == 0 ? v[0] : i == 1 ? v[1] : i == 2 ? v[2] : i == 3 ? v[3] : i == 4 ? v[4] : v[5];
-}
-
-// Warp -> work.  Warps 0 .. n_stripes*n_segs-1 take (stripe, segment) as
-// the plain kernels do; with halving on, an edge segment keeps only its first
-// half there and the warps after them take the second halves, first the edge
-// stripes' segments (nc * n_segs), then the edge segments of the other
-// stripes ((n_stripes - nc) * nr).
+// Warp -> work: plain_work for every kernel.  With the TF/SF source on, all
+// warps carry the edge logic in their general iterations (TF = true); the
+// interior iterations skip it where no edge can be met.
 template <int K, int CPL, bool LOSSY, bool PML, int WARPS, int TRACE, int NFC>
 __global__ void __launch_bounds__(WARPS * 32, CPL == 2 ? (NFC == kPlain ? 4 : kExtMinBlocks) : 1)
     k_march(const MarchArgs a) {
   const int gw = blockIdx.x * WARPS + (threadIdx.x >> 5);
-  const int n_base = a.n_stripes * a.n_segs;
   if constexpr (NFC == kPlain) {
     int stripe, i_s, i_e;
     if (!plain_work(a, gw, stripe, i_s, i_e)) return;  // whole warp leaves; nothing below syncs the block
     march_body<K, CPL, LOSSY, PML, WARPS, TRACE, NFC, false>(a, stripe, i_s, i_e);
   } else {
-    const int np = a.ext.tfsf_npml;
-    const int nc = a.ext.nc, nr = a.ext.nr;
-    int stripe, seg, half = 0;  // 0: whole segment, 1: first half, 2: second half
-    if (gw < n_base) {
-      stripe = gw % a.n_stripes;
-      seg = gw / a.n_stripes;
-    } else {
-      int k = gw - n_base;
-      if (k < nc * a.n_segs) {
-        stripe = pick6(a.ext.tf_c, k / a.n_segs);
-        seg = k % a.n_segs;
-      } else {
-        k -= nc * a.n_segs;
-        if (k >= (a.n_stripes - nc) * nr) return;
-        seg = pick6(a.ext.tf_r, k % nr);
-        stripe = k / nr;  // the stripe-th stripe not in tf_c (ascending)
-        for (int i = 0; i < nc; ++i)
-          if (pick6(a.ext.tf_c, i) <= stripe) ++stripe;
-      }
-      half = 2;
-    }
-    const bool tf = np > 0 && (tf_stripe<CPL>(np, a.ny, stripe) || tf_segment<K>(np, a.nx, a.seg_rows, seg));
-    if (tf && half == 0 && (nc > 0 || nr > 0)) half = 1;
-    int i_s = seg * a.seg_rows;
-    int i_e = min(a.nx, i_s + a.seg_rows);
-    const int mid = i_s + (i_e - i_s + 1) / 2;
-    if (half == 1) i_e = mid;
-    if (half == 2) i_s = mid;
-    if (i_s >= i_e) return;
-    if (tf)
+    int stripe, i_s, i_e;
+    if (!plain_work(a, gw, stripe, i_s, i_e)) return;
+    if (a.ext.tfsf_npml > 0)
       march_body<K, CPL, LOSSY, PML, WARPS, TRACE, NFC, true>(a, stripe, i_s, i_e);
     else
       march_body<K, CPL, LOSSY, PML, WARPS, TRACE, NFC, false>(a, stripe, i_s, i_e);
   }
 }
 
-// Work layout of the plain kernels' single wave of warps (MarchArgs).  The
+// Work layout of the fused kernels' single wave of warps (MarchArgs).  The
 // stripes that reach column 0, column ny-1 or (with the pml_hint) the
-// absorbing layer run general iterations throughout; they get gen_cost times
+// absorbing layer or the TF/SF box's edge columns run general iterations
+// throughout; they get gen_cost times
 // as many segments.  In the other stripes only the rows of the layer and the
 // grid's first/last rows (plus the K-row cone) iterate in the general form,
 // so their first and last segments are shortened by that extra time.
 template <int K, int CPL>
 long plain_layout(MarchArgs& a, long resident, float G) {
   constexpr int W = 32 * CPL, OUTW = W - 2 * HALO;
-  const int P = a.pml_hint > 0 ? a.pml_hint : 0;
+  // the absorbing layer and, with TF/SF on, the box's edges (at np-2 ..
+  // n-np, next to the layer in the reference's programs)
+  const int P = std::max(a.pml_hint > 0 ? a.pml_hint : 0, a.ext.tfsf_npml > 0 ? a.ext.tfsf_npml + 1 : 0);
   auto general = [&](int s) {
     const int lo = s * OUTW - HALO, hi = lo + W - 1;
     return lo < std::max(P, 1) || hi > a.ny - 2 - P;
@@ -864,13 +827,6 @@ int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
     resident = (long)nsm * blocks_per_sm * WARPS;
     // one wave of warps: n_stripes * n_segs ~= resident warps
     long n_segs = resident / a.n_stripes;
-    if (EXT && a.ext.tfsf_npml > 0) {
-      // room for the halved edge segments: every segment of the edge
-      // stripes, and about 4 edge segments of the other stripes
-      int nc = 0;
-      for (int q = 0; q < a.n_stripes; ++q) nc += tf_stripe<CPL>(a.ext.tfsf_npml, a.ny, q) ? 1 : 0;
-      n_segs = (resident - 4L * (a.n_stripes - nc)) / (a.n_stripes + nc);
-    }
     if (n_segs < 1) n_segs = 1;
     seg_rows = (int)((a.nx + n_segs - 1) / n_segs);
     // keep the recomputed cone (2K rows per segment) small
@@ -883,31 +839,8 @@ int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
   a.seg_rows_g = seg_rows;
   a.n_segs_g = 0;
   long warps = (long)a.n_stripes * a.n_segs;
-  if (!EXT && resident > 0)
+  if (resident > 0)
     warps = plain_layout<K, CPL>(a, resident, g_cfg.gen_cost > 0.f ? g_cfg.gen_cost : (CPL == 4 ? 4.0f : 2.5f));
-  if (EXT) {
-    a.ext.nc = a.ext.nr = 0;
-    const int np = a.ext.tfsf_npml;
-    if (np > 0) {
-      int nc = 0, nr = 0;
-      bool fits = true;
-      for (int q = 0; q < a.n_stripes && fits; ++q)
-        if (tf_stripe<CPL>(np, a.ny, q)) {
-          if (nc == 6) fits = false;
-          else a.ext.tf_c[nc++] = q;
-        }
-      for (int q = 0; q < a.n_segs && fits; ++q)
-        if (tf_segment<K>(np, a.nx, a.seg_rows, q)) {
-          if (nr == 6) fits = false;
-          else a.ext.tf_r[nr++] = q;
-        }
-      if (fits) {  // otherwise edge segments run whole
-        a.ext.nc = nc;
-        a.ext.nr = nr;
-        warps += (long)nc * a.n_segs + (long)(a.n_stripes - nc) * nr;
-      }
-    }
-  }
   const int blocks = (int)((warps + WARPS - 1) / WARPS);
   kern<<<blocks, WARPS * 32, smem, st>>>(a);
   return fdtd_host::check_launch();

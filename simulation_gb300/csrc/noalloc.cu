@@ -23,7 +23,10 @@
 //     fit beside the fields: those runs go one step per fdtd2d_step_n call
 //     (its three-launch form, which needs no workspace);
 //   * the first call on a device resolves the array's address with
-//     cudaGetSymbolAddress; make that first call before any stream capture;
+//     cudaGetSymbolAddress; with lazy module loading that is when the driver
+//     reserves the array, so the first call can fail with FDTD_ERR_CUDA when
+//     the device is out of memory: make it up front, before any stream
+//     capture; the address is kept for the process (no cudaDeviceReset);
 //   * all calls share the one array and it keeps the last call's contents;
 //     nothing in it has to start at zero (each call's first pass overwrites
 //     it before reading it), but calls whose work overlaps on the GPU (two
@@ -71,12 +74,18 @@ int scratch_address(void** out) {
 extern "C" int fdtd2d_step_n_noalloc(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps,
                                      int steps_per_pass, fdtd_stream_t stream) {
   if (!p || !s) return FDTD_ERR_NULL;
+  if (t0 < 0 || nsteps < 0) return FDTD_ERR_ARG;  // as fdtd2d_step_n, before either path
   if ((long long)p->nx * p->ny > (long long)FDTD2D_NOALLOC_MAX_CELLS) return FDTD_ERR_SIZE;
   const size_t need = fdtd2d_workspace_size(p, steps_per_pass);
   if (need > kScratchBytes) {
     if (p->tfsf_npml <= 0 && p->nf <= 0) return FDTD_ERR_SIZE;
+    // one-step calls (three launches each, no workspace); the Inf/NaN test,
+    // which every call would otherwise run, runs once after the last step
+    fdtd2d_state quiet = *s;
+    quiet.status = nullptr;
     for (int i = 0; i < nsteps; ++i) {
-      const int rc = fdtd2d_step_n(p, s, t0 + i, 1, steps_per_pass, nullptr, 0, stream);
+      const int rc = fdtd2d_step_n(p, i + 1 == nsteps ? s : &quiet, t0 + i, 1, steps_per_pass, nullptr, 0,
+                                   stream);
       if (rc != FDTD_OK) return rc;
     }
     return FDTD_OK;

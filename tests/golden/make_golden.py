@@ -20,6 +20,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+# the development container's checkout unless FDTD_REFERENCE_ROOT names another
+os.environ.setdefault("FDTD_REFERENCE_ROOT", "/root/reference")
 
 from oracle import refload  # noqa: E402
 

@@ -1,11 +1,12 @@
-"""Warp -> work mapping of the fused pass with TF/SF, checked on the CPU.
+"""Warp -> work layout of the fused passes, checked on the CPU.
 
-The fused pass compiles the TF/SF edge logic only into the body that edge
-warps run and halves their segments across extra warps.  The check program
-(tests/march_mapping_check.cu) includes the kernel header, uses its own
-tf_stripe / tf_segment predicates, and verifies over many grid shapes, PML
-widths, segment lengths and steps per pass that every (stripe, row) is owned
-exactly once and that no warp classified as plain reaches an edge cell.  It
+One launch is a single wave of warps; the stripes and segments that hold
+the absorbing layer, the grid's edges or the TF/SF box's edge columns get
+shorter work.  The check program (tests/march_mapping_check.cu) includes the
+kernel header and calls its own plain_layout / plain_work over many grid
+shapes, layer widths, TF/SF boxes, wave sizes, cost factors and steps per
+pass: every (stripe, row) is owned by exactly one warp, every warp's work is
+inside the grid, and every instantiation's shared memory fits a block.  It
 is host code only: built with nvcc, run here, no GPU needed.
 """
 import os
@@ -17,7 +18,7 @@ import pytest
 from tests.conftest import ROOT
 
 
-def test_tfsf_edge_classification_and_coverage(tmp_path):
+def test_work_layout_coverage_and_shared_memory(tmp_path):
     nvcc = shutil.which("nvcc") or ("/usr/local/cuda/bin/nvcc" if os.path.exists("/usr/local/cuda/bin/nvcc") else None)
     if nvcc is None:
         pytest.skip("nvcc not available")
