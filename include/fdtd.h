@@ -337,6 +337,13 @@ int fno_lift_bwd(long long rows, int C, int cin, const float* in, const void* dx
 int fno_propagation(int n, int nbins, const float* feat, int nf, const double* wdt, double eps_scale,
                     double sig_scale, double loss_scale, int probe_in, int probe_gap, float* P,
                     fdtd_stream_t stream);
+/* Network inputs from slab layer tables (device arrays, the batched runs'
+ * layout): out [n][nbins][6] float32, (eps_r-1)/eps_scale of cells 2b-1, 2b,
+ * 2b+1 of run run_idx[q] (run q when run_idx is NULL), then sigma/sig_scale of
+ * the same cells; cells outside every layer are vacuum (0). */
+int fno_profile_features(int n, const int* run_idx, const int* layer_off, const int* layer_start,
+                         const int* layer_end, const double* epsr, const double* sigma, int nbins, double eps_scale,
+                         double sig_scale, float* out, fdtd_stream_t stream);
 /* out = P (.) y, or conj(P) (.) y when conj_p, for n spectra stored [Re(nf) | Im(nf)] */
 int fno_cmul(long long n, int nf, const float* P, const float* y, int conj_p, float* out, fdtd_stream_t stream);
 int fno_dft_to_modes(int B, int C, int M, const float* F, void* Fm, fdtd_stream_t stream);

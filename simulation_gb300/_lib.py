@@ -140,6 +140,7 @@ _SIGS = {
     "fdtd2d_tm_adjoint_reverse": ([C.POINTER(Params2D), C.POINTER(AdjointParams2D), F, F, P, C.c_size_t, P],
                                   C.c_int),
     "fdtd2d_tm_adjoint": ([C.POINTER(Params2D), C.POINTER(AdjointParams2D), F, P, F, F, P, C.c_size_t, P], C.c_int),
+    "fno_profile_features": ([C.c_int, P, P, P, P, P, P, C.c_int, C.c_double, C.c_double, F, P], C.c_int),
     "fdtd_dft_amplitude_phase": ([C.c_int, C.c_longlong, F, F, C.c_longlong, F, F, P, P, P], C.c_int),
     "fdtd2d_step_n_noalloc": ([C.POINTER(Params2D), C.POINTER(State2D), C.c_int, C.c_int, C.c_int, P], C.c_int),
     "fdtd2d_dielectric_cylinder": ([C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,

@@ -221,6 +221,13 @@ class BatchRunner:
             _lib.call("fdtd1d_batch_run", C.byref(p), C.byref(o), pl.data_ptr(), n, nb, grp["cpt"], grp["block"],
                       grp.get("ctas_per_sm", 0), max_cycles, st)
 
+    def spectrum(self) -> torch.Tensor:
+        """[nruns][2*nf] float32 on the device: (Re T | Im T) of T(f) =
+        DFT_exit/DFT_entry, divided in double (no host round trip)."""
+        s = self.spec.double()
+        T = torch.complex(s[:, 2], s[:, 3]) / torch.complex(s[:, 0], s[:, 1])
+        return torch.cat([T.real, T.imag], dim=1).float()
+
     def transmission(self):
         """Complex T(f) = DFT_exit/DFT_entry per run, float64 [nruns][nf]."""
         s = self.spec.double().cpu().numpy()

@@ -47,22 +47,43 @@ struct AdjArgs {
   float* grad_nbz;
 };
 
-__device__ __forceinline__ float lam_cx(const AdjArgs& a, int i, int j) {
+// Where the per-cell functions below read the state: straight from global
+// memory (GlobalCells), or from a block's shared-memory copy of its tile and
+// halo (TileCells).  Both give the same values, so every form of the reverse
+// step does the same arithmetic on the same operands.
+struct GlobalCells {
+  const AdjArgs& a;
+  __device__ __forceinline__ size_t n(int i, int j) const { return (size_t)i * a.ny + j; }
+  __device__ __forceinline__ float fdz(int i, int j) const { return __ldg(a.fwd.dz + n(i, j)); }
+  __device__ __forceinline__ float fiz(int i, int j) const { return __ldg(a.fwd.iz + n(i, j)); }
+  __device__ __forceinline__ float fhx(int i, int j) const { return __ldg(a.fwd.hx + n(i, j)); }
+  __device__ __forceinline__ float fhy(int i, int j) const { return __ldg(a.fwd.hy + n(i, j)); }
+  __device__ __forceinline__ float naz(int i, int j) const { return __ldg(a.naz + n(i, j)); }
+  __device__ __forceinline__ float nbz(int i, int j) const { return __ldg(a.nbz + n(i, j)); }
+  __device__ __forceinline__ float ldz(int i, int j) const { return __ldg(a.adj.dz + n(i, j)); }
+  __device__ __forceinline__ float liz(int i, int j) const { return __ldg(a.adj.iz + n(i, j)); }
+  __device__ __forceinline__ float lhx(int i, int j) const { return __ldg(a.adj.hx + n(i, j)); }
+  __device__ __forceinline__ float lhy(int i, int j) const { return __ldg(a.adj.hy + n(i, j)); }
+  __device__ __forceinline__ float lihx(int i, int j) const { return __ldg(a.adj.ihx + n(i, j)); }
+  __device__ __forceinline__ float lihy(int i, int j) const { return __ldg(a.adj.ihy + n(i, j)); }
+};
+
+template <class Cells>
+__device__ __forceinline__ float lam_cx(const AdjArgs& a, const Cells& c, int i, int j) {
   // adjoint of cx at (i, j) from hx', ihx' there (0 where H is not applied)
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
-  const size_t n = (size_t)i * a.ny + j;
-  const float lhx = __ldg(a.adj.hx + n);
+  const float lhx = c.lhx(i, j);
   const float fy2 = __ldg(a.pml.fy2 + j);
-  const float lihx_t = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, __ldg(a.adj.ihx + n));
+  const float lihx_t = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, c.lihx(i, j));
   return __fmaf_rn(__fmul_rn(0.5f, fy2), lhx, lihx_t);
 }
 
-__device__ __forceinline__ float lam_cy(const AdjArgs& a, int i, int j) {
+template <class Cells>
+__device__ __forceinline__ float lam_cy(const AdjArgs& a, const Cells& c, int i, int j) {
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
-  const size_t n = (size_t)i * a.ny + j;
-  const float lhy = __ldg(a.adj.hy + n);
+  const float lhy = c.lhy(i, j);
   const float fx2 = __ldg(a.pml.fx2 + i);
-  const float lihy_t = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, __ldg(a.adj.ihy + n));
+  const float lihy_t = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, c.lihy(i, j));
   return __fmaf_rn(-__fmul_rn(0.5f, fx2), lhy, lihy_t);
 }
 
@@ -72,28 +93,28 @@ __device__ __forceinline__ float lam_cy(const AdjArgs& a, int i, int j) {
 // before the D update is undone.  With `own`, also writes L(iz) and adds the
 // cell's dJ/dnaz, dJ/dnbz (a cell computed only as a neighbour's halo does
 // neither).
-__device__ __forceinline__ float adj_e(const AdjArgs& a, int i, int j, bool own) {
+template <class Cells>
+__device__ __forceinline__ float adj_e(const AdjArgs& a, const Cells& c, int i, int j, bool own) {
   const size_t n = (size_t)i * a.ny + j;
   // forward recompute of dz' and ez at this cell (same formulas as the forward)
-  float dzp = __ldg(a.fwd.dz + n);
+  float dzp = c.fdz(i, j);
   if (i >= 1 && j >= 1)
-    dzp = d_update(dzp, __ldg(a.fwd.hy + n), __ldg(a.fwd.hy + n - a.ny), __ldg(a.fwd.hx + n),
-                   __ldg(a.fwd.hx + n - 1), __ldg(a.pml.gx3 + i),
+    dzp = d_update(dzp, c.fhy(i, j), c.fhy(i - 1, j), c.fhx(i, j), c.fhx(i, j - 1), __ldg(a.pml.gx3 + i),
                    __ldg(a.pml.gy3 + j), __ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j));
   if (a.src_kind != FDTD_SRC_NONE && i == a.src_i && j == a.src_j) {
     const float v = __ldg(a.src_table + a.t - 1);
     dzp = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(dzp, v);
   }
-  const float izv = a.nbz ? __ldg(a.fwd.iz + n) : 0.f;
+  const float izv = a.nbz ? c.fiz(i, j) : 0.f;
   const float diff = __fsub_rn(dzp, izv);
-  const float naz = __ldg(a.naz + n);
+  const float naz = c.naz(i, j);
   const float ez = __fmul_rn(naz, diff);
   // adjoint of ez
-  float lez = lam_cx(a, i, j) - lam_cx(a, i, j - 1) + lam_cy(a, i, j) - lam_cy(a, i - 1, j);
+  float lez = lam_cx(a, c, i, j) - lam_cx(a, c, i, j - 1) + lam_cy(a, c, i, j) - lam_cy(a, c, i - 1, j);
   if (i == a.probe_i && j == a.probe_j) lez = __fmaf_rn(a.probe_w, ez, lez);
   // E backward
-  const float nbz = a.nbz ? __ldg(a.nbz + n) : 0.f;
-  const float liz = a.nbz ? __ldg(a.adj.iz + n) : 0.f;
+  const float nbz = a.nbz ? c.nbz(i, j) : 0.f;
+  const float liz = a.nbz ? c.liz(i, j) : 0.f;
   const float lezt = __fmaf_rn(nbz, liz, lez);
   if (own) {
     if (a.nbz) a.out.iz[n] = __fmaf_rn(-naz, lezt, liz);
@@ -104,7 +125,7 @@ __device__ __forceinline__ float adj_e(const AdjArgs& a, int i, int j, bool own)
       if (a.grad_nbz) a.grad_nbz[b] = __fmaf_rn(liz, ez, a.grad_nbz[b]);
     }
   }
-  return __fmaf_rn(naz, lezt, __ldg(a.adj.dz + n));
+  return __fmaf_rn(naz, lezt, c.ldz(i, j));
 }
 
 // cb*T at (i, j): the D adjoint flowing into the curl's H terms (0 where D is
@@ -119,7 +140,8 @@ __device__ __forceinline__ float dgrad(const AdjArgs& a, int i, int j, float T) 
 // D and H part of the reverse step at one cell, given T there (T) and at
 // the (i+1, j) and (i, j+1) neighbours (Ti, Tj): L(dz) = ca*T, L(hy) +=
 // cb*T - cb[i+1]*T[i+1], L(hx) += -cb*T + cb[j+1]*T[j+1], then H backward.
-__device__ __forceinline__ void adj_dh(const AdjArgs& a, int i, int j, float T, float Ti, float Tj) {
+template <class Cells>
+__device__ __forceinline__ void adj_dh(const AdjArgs& a, const Cells& c, int i, int j, float T, float Ti, float Tj) {
   const size_t n = (size_t)i * a.ny + j;
   const bool hard_src = (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j);
   float ldz;
@@ -128,8 +150,7 @@ __device__ __forceinline__ void adj_dh(const AdjArgs& a, int i, int j, float T, 
   else ldz = T;
   const float dg = dgrad(a, i, j, T);
   const bool hm = (i <= a.nx - 2) && (j <= a.ny - 2);
-  float lhx = __ldg(a.adj.hx + n), lhy = __ldg(a.adj.hy + n), lihx = __ldg(a.adj.ihx + n),
-        lihy = __ldg(a.adj.ihy + n);
+  float lhx = c.lhx(i, j), lhy = c.lhy(i, j), lihx = c.lihx(i, j), lihy = c.lihy(i, j);
   if (hm) {
     const float fy2 = __ldg(a.pml.fy2 + j), fx2 = __ldg(a.pml.fx2 + i);
     lihx = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, lihx);
@@ -151,7 +172,7 @@ __global__ void k_adj_a(const AdjArgs a) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= a.nx || j >= a.ny) return;
-  a.tmp[(size_t)i * a.ny + j] = adj_e(a, i, j, true);
+  a.tmp[(size_t)i * a.ny + j] = adj_e(a, GlobalCells{a}, i, j, true);
 }
 
 __global__ void k_adj_b(const AdjArgs a) {
@@ -161,46 +182,95 @@ __global__ void k_adj_b(const AdjArgs a) {
   const size_t n = (size_t)i * a.ny + j;
   const float Ti = (i + 1 < a.nx) ? a.tmp[n + a.ny] : 0.f;
   const float Tj = (j + 1 < a.ny) ? a.tmp[n + 1] : 0.f;
-  adj_dh(a, i, j, a.tmp[n], Ti, Tj);
+  adj_dh(a, GlobalCells{a}, i, j, a.tmp[n], Ti, Tj);
 }
 
-// Fused form: one block of 32 x 8 threads takes a kAdjTI x 32 tile (each
-// thread kAdjTI/8 rows), computes T on the tile plus one row and one column
-// of halo into shared memory (warps 0 and 1 and one lane of warp 2 take the
-// halo), then runs the D/H part for the tile.  It reads the adjoints after
-// step t (a.adj) and writes those before it to other arrays (a.out): a halo
-// cell's inputs belong to the neighbouring tile, which must not have
-// overwritten them.  Same per-cell arithmetic as the two-kernel form, so the
-// results are bitwise equal.
+// Fused form: one block of 32 x 8 threads takes a kAdjTI x 32 tile.  It first
+// copies every value the step reads for the tile, one row and one column of
+// halo below and right of it (whose T it needs) and one row and one column
+// above and left of that (their neighbours), into shared memory: twelve
+// fields over (kAdjTI+2) x 34 cells, all loads independent and issued
+// together.  Then it computes T on the tile and halo, then the D/H part for
+// the tile.  It reads the adjoints after step t (a.adj) and writes those
+// before it to other arrays (a.out): a halo cell's inputs belong to the
+// neighbouring tile, which must not have overwritten them.  Same per-cell
+// arithmetic on the same values as the two-kernel form, so the results are
+// bitwise equal.  Cells outside the grid are staged as 0 and never used
+// (every use is guarded by the grid bounds as in the global form).
 constexpr int kAdjTJ = 32, kAdjTI = 16, kAdjThreadsY = 8, kAdjRows = kAdjTI / kAdjThreadsY;
+// staged rows i0-1 .. i0+TI and columns j0-4 .. j0+TJ+3: the columns the
+// step reads are j0-1 .. j0+TJ; the tile is widened to whole 16-byte groups
+// so it is copied with one float4 load per field and group (ny % 4 == 0)
+constexpr int kTileR = kAdjTI + 2, kTileC = kAdjTJ + 8, kTileQ = kTileC / 4;
+enum { F_FDZ, F_FIZ, F_FHX, F_FHY, F_NAZ, F_NBZ, F_LDZ, F_LIZ, F_LHX, F_LHY, F_LIHX, F_LIHY, F_COUNT };
+
+struct TileCells {
+  const float (*t)[kTileR][kTileC];  // [field][row][column]
+  int i0, j0;
+  __device__ __forceinline__ float at(int f, int i, int j) const { return t[f][i - i0 + 1][j - j0 + 4]; }
+  __device__ __forceinline__ float fdz(int i, int j) const { return at(F_FDZ, i, j); }
+  __device__ __forceinline__ float fiz(int i, int j) const { return at(F_FIZ, i, j); }
+  __device__ __forceinline__ float fhx(int i, int j) const { return at(F_FHX, i, j); }
+  __device__ __forceinline__ float fhy(int i, int j) const { return at(F_FHY, i, j); }
+  __device__ __forceinline__ float naz(int i, int j) const { return at(F_NAZ, i, j); }
+  __device__ __forceinline__ float nbz(int i, int j) const { return at(F_NBZ, i, j); }
+  __device__ __forceinline__ float ldz(int i, int j) const { return at(F_LDZ, i, j); }
+  __device__ __forceinline__ float liz(int i, int j) const { return at(F_LIZ, i, j); }
+  __device__ __forceinline__ float lhx(int i, int j) const { return at(F_LHX, i, j); }
+  __device__ __forceinline__ float lhy(int i, int j) const { return at(F_LHY, i, j); }
+  __device__ __forceinline__ float lihx(int i, int j) const { return at(F_LIHX, i, j); }
+  __device__ __forceinline__ float lihy(int i, int j) const { return at(F_LIHY, i, j); }
+};
+
 __global__ void __launch_bounds__(kAdjTJ * kAdjThreadsY) k_adj_fused(const AdjArgs a) {
-  __shared__ float sT[kAdjTI + 1][kAdjTJ + 1];
+  extern __shared__ float adj_smem[];
+  float (*tile)[kTileR][kTileC] = reinterpret_cast<float (*)[kTileR][kTileC]>(adj_smem);
+  float (*sT)[kAdjTJ + 1] = reinterpret_cast<float (*)[kAdjTJ + 1]>(adj_smem + F_COUNT * kTileR * kTileC);
   const int j0 = blockIdx.x * kAdjTJ, i0 = blockIdx.y * kAdjTI;
+  const int tid = threadIdx.y * kAdjTJ + threadIdx.x;
+  const float* src[F_COUNT] = {a.fwd.dz, a.fwd.iz, a.fwd.hx, a.fwd.hy, a.naz, a.nbz,
+                               a.adj.dz, a.adj.iz, a.adj.hx, a.adj.hy, a.adj.ihx, a.adj.ihy};
+  static_assert(kTileR * kTileQ <= kAdjTJ * kAdjThreadsY, "one float4 group per thread and field");
+  if (tid < kTileR * kTileQ) {
+    const int r = tid / kTileQ, q = tid - r * kTileQ;
+    const int i = i0 - 1 + r, j = j0 - 4 + 4 * q;
+    const bool in = i >= 0 && i < a.nx && j >= 0 && j < a.ny;  // a group is wholly in or out
+    const size_t n = in ? (size_t)i * a.ny + j : 0;
+    float4 v[F_COUNT];
+#pragma unroll
+    for (int f = 0; f < F_COUNT; ++f)
+      v[f] = (in && src[f]) ? __ldg(reinterpret_cast<const float4*>(src[f] + n)) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int f = 0; f < F_COUNT; ++f) *reinterpret_cast<float4*>(&tile[f][r][4 * q]) = v[f];
+  }
+  __syncthreads();
+  const TileCells c{tile, i0, j0};
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int j = j0 + tx;
 #pragma unroll
   for (int k = 0; k < kAdjRows; ++k) {
     const int li = ty + kAdjThreadsY * k, i = i0 + li;
-    sT[li][tx] = (i < a.nx && j < a.ny) ? adj_e(a, i, j, true) : 0.f;
+    sT[li][tx] = (i < a.nx && j < a.ny) ? adj_e(a, c, i, j, true) : 0.f;
   }
   if (ty == 0) {  // halo row below the tile
     const int i = i0 + kAdjTI;
-    sT[kAdjTI][tx] = (i < a.nx && j < a.ny) ? adj_e(a, i, j, false) : 0.f;
+    sT[kAdjTI][tx] = (i < a.nx && j < a.ny) ? adj_e(a, c, i, j, false) : 0.f;
   } else if (ty == 1 && tx < kAdjTI) {  // halo column right of the tile
     const int i = i0 + tx, jj = j0 + kAdjTJ;
-    sT[tx][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, i, jj, false) : 0.f;
+    sT[tx][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, c, i, jj, false) : 0.f;
   } else if (ty == 2 && tx == 0) {  // and their corner
     const int i = i0 + kAdjTI, jj = j0 + kAdjTJ;
-    sT[kAdjTI][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, i, jj, false) : 0.f;
+    sT[kAdjTI][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, c, i, jj, false) : 0.f;
   }
   __syncthreads();
   if (j >= a.ny) return;
 #pragma unroll
   for (int k = 0; k < kAdjRows; ++k) {
     const int li = ty + kAdjThreadsY * k, i = i0 + li;
-    if (i < a.nx) adj_dh(a, i, j, sT[li][tx], sT[li + 1][tx], sT[li][tx + 1]);
+    if (i < a.nx) adj_dh(a, c, i, j, sT[li][tx], sT[li + 1][tx], sT[li][tx + 1]);
   }
 }
+constexpr size_t kAdjSmem = (size_t)(F_COUNT * kTileR * kTileC + (kAdjTI + 1) * (kAdjTJ + 1)) * sizeof(float);
 
 }  // namespace
 
@@ -232,7 +302,7 @@ int launch_adjoint_fused(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd
   a.grad_nbz = grad_nbz;
   const dim3 blk(kAdjTJ, kAdjThreadsY);
   const dim3 grd((p.ny + kAdjTJ - 1) / kAdjTJ, (p.nx + kAdjTI - 1) / kAdjTI);
-  k_adj_fused<<<grd, blk, 0, st>>>(a);
+  k_adj_fused<<<grd, blk, kAdjSmem, st>>>(a);
   return fdtd_host::check_launch();
 }
 

@@ -839,8 +839,12 @@ int launch_t(const MarchArgs& a0, int warps_cfg, int seg_cfg, cudaStream_t st) {
   a.seg_rows_g = seg_rows;
   a.n_segs_g = 0;
   long warps = (long)a.n_stripes * a.n_segs;
-  if (resident > 0)
-    warps = plain_layout<K, CPL>(a, resident, g_cfg.gen_cost > 0.f ? g_cfg.gen_cost : (CPL == 4 ? 4.0f : 2.5f));
+  if (resident > 0) {
+    // measured defaults: plain 128-column 4.0, plain 64-column 2.5, with the
+    // fd2d_3_4 extras 2.0 (2048^2: 108.6 Gcell/s; 84 at 1, 94-105 at 2.5-3)
+    const float G = g_cfg.gen_cost > 0.f ? g_cfg.gen_cost : (EXT ? 2.0f : (CPL == 4 ? 4.0f : 2.5f));
+    warps = plain_layout<K, CPL>(a, resident, G);
+  }
   const int blocks = (int)((warps + WARPS - 1) / WARPS);
   kern<<<blocks, WARPS * 32, smem, st>>>(a);
   return fdtd_host::check_launch();

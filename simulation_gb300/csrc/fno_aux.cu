@@ -32,6 +32,41 @@ __device__ __forceinline__ float gelu_grad(float z) {
   return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * fmaf(0.134145f * z, z, 1.0f);
 }
 
+// Network inputs of slab profiles, built from their layer tables (the
+// surrogate's profile_features): out[q][b][0..2] = (eps_r - 1)/eps_scale of
+// cells 2b-1, 2b, 2b+1 of run run_idx[q], out[q][b][3..5] = sigma/sig_scale
+// of the same cells; cells in no layer (or before cell 0) are vacuum, 0.
+// The quotients are formed in double and rounded once, as the host form does.
+__global__ void k_profile_features(int n, const int* __restrict__ run_idx, const int* __restrict__ layer_off,
+                                   const int* __restrict__ layer_start, const int* __restrict__ layer_end,
+                                   const double* __restrict__ epsr, const double* __restrict__ sigma, int nbins,
+                                   double eps_scale, double sig_scale, float* __restrict__ out) {
+  const long long total = (long long)n * nbins;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int q = (int)(x / nbins), b = (int)(x - (long long)q * nbins);
+    const int r = run_idx ? run_idx[q] : q;
+    const int l0 = layer_off[r], l1 = layer_off[r + 1];
+    float v[6];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int cell = 2 * b - 1 + c;
+      double e = 0.0, g = 0.0;
+      for (int l = l0; l < l1; ++l)
+        if (cell >= layer_start[l] && cell < layer_end[l]) {
+          e = (epsr[l] - 1.0) / eps_scale;
+          g = sigma[l] / sig_scale;
+        }
+      v[c] = (float)e;
+      v[3 + c] = (float)g;
+    }
+    float2* o = reinterpret_cast<float2*>(out + x * 6);
+    o[0] = make_float2(v[0], v[1]);
+    o[1] = make_float2(v[2], v[3]);
+    o[2] = make_float2(v[4], v[5]);
+  }
+}
+
 inline dim3 grid1(size_t n, int t = 256) {
   size_t b = (n + t - 1) / t;
   if (b > 152 * 64) b = 152 * 64;
@@ -676,6 +711,16 @@ int fno_propagation(int n, int nbins, const float* feat, int nf, const double* w
   const long long threads = 32LL * n;
   FNO_LAUNCH(fdtd::k_propagation, dim3((unsigned)((threads + 255) / 256)), 256, n, nbins, feat, nf, wdt, eps_scale,
              sig_scale, loss_scale, probe_in, probe_gap, P);
+}
+
+int fno_profile_features(int n, const int* run_idx, const int* layer_off, const int* layer_start,
+                         const int* layer_end, const double* epsr, const double* sigma, int nbins, double eps_scale,
+                         double sig_scale, float* out, fdtd_stream_t stream) {
+  if (!layer_off || !layer_start || !layer_end || !epsr || !sigma || !out) return FDTD_ERR_NULL;
+  if (n < 1 || nbins < 1 || !(eps_scale > 0) || !(sig_scale > 0)) return FDTD_ERR_SIZE;
+  if ((uintptr_t)out & 7) return FDTD_ERR_ALIGN;
+  FNO_LAUNCH(fdtd::k_profile_features, fdtd::grid1((size_t)n * nbins), 256, n, run_idx, layer_off, layer_start,
+             layer_end, epsr, sigma, nbins, eps_scale, sig_scale, out);
 }
 
 int fno_cmul(long long n, int nf, const float* P, const float* y, int conj_p, float* out, fdtd_stream_t stream) {

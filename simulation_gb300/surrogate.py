@@ -102,6 +102,31 @@ def profile_features(batch: "B1.SlabBatch", idx=None, nbins: int = NBINS) -> np.
     return out
 
 
+def device_features(batch: "B1.SlabBatch", idx=None, nbins: int = NBINS, device="cuda") -> torch.Tensor:
+    """``profile_features`` built on the device from the batch's layer tables
+    (``fno_profile_features``): [n][nbins][6] float32, bitwise the same values.
+    The tables are copied to the device once per batch object."""
+    dev = torch.device(device)
+    tabs = getattr(batch, "_feature_tables", None)
+    if tabs is None or tabs[0].device != dev:
+        i32 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32)).to(dev)  # noqa: E731
+        f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(dev)  # noqa: E731
+        pad = lambda a: a if a.size else np.zeros(1)  # noqa: E731
+        tabs = (i32(batch.layer_off), i32(pad(batch.layer_start)), i32(pad(batch.layer_end)), f64(pad(batch.epsr)),
+                f64(pad(batch.sigma)))
+        batch._feature_tables = tabs
+    idx_t = None
+    n = batch.nruns
+    if idx is not None:
+        idx_t = torch.as_tensor(np.ascontiguousarray(idx, dtype=np.int32)).to(dev)
+        n = idx_t.numel()
+    out = torch.empty((n, nbins, CIN), dtype=torch.float32, device=dev)
+    if n:
+        _call("fno_profile_features", n, None if idx_t is None else idx_t.data_ptr(), *(t.data_ptr() for t in tabs),
+              nbins, EPS_SCALE, SIG_SCALE, out.data_ptr())
+    return out
+
+
 _WDT = {}
 
 
@@ -450,14 +475,36 @@ def solve_fdtd(batch: "B1.SlabBatch", nsteps: int = NSTEPS, chunk: int = 4096, d
     return out
 
 
-def generate_dataset(n: int, seed: int, nsteps: int = NSTEPS, chunk: int = 4096, device="cuda"):
+def solve_fdtd_device(batch: "B1.SlabBatch", nsteps: int = NSTEPS, device="cuda") -> torch.Tensor:
+    """``solve_fdtd`` left on the device, enqueued on the current stream: [n][128]."""
+    r = B1.BatchRunner(batch, nsteps=nsteps, freqs=FREQS, wave=WAVE, device=device)
+    r.run()
+    return r.spectrum()
+
+
+def rel_l2_spectrum_device(pred: torch.Tensor, ref: torch.Tensor, floor: float = SPECTRUM_FLOOR) -> torch.Tensor:
+    """``rel_l2_spectrum`` on device tensors (float64 norms)."""
+    nf = ref.shape[1] // 2
+    den = torch.clamp(torch.linalg.vector_norm(ref.double(), dim=1), min=floor * math.sqrt(nf))
+    return torch.linalg.vector_norm((pred - ref).double(), dim=1) / den
+
+
+def generate_dataset(n: int, seed: int, nsteps: int = NSTEPS, chunk: int = 4096, device="cuda",
+                     on_device: bool = False):
     """Slab runs of the batched-FDTD distribution solved by the batched kernel:
-    returns (inputs [n][NBINS][6], targets [n][128], batch)."""
+    returns (inputs [n][NBINS][6], targets [n][128], batch), as host arrays,
+    or (on_device) as device tensors built and kept on the GPU."""
     batch = B1.slab_batch(n, seed=seed)
     if np.any(batch.probe_in != PROBE_IN) or np.any(batch.probe_out != batch.layer_end[batch.layer_off[1:] - 1]
                                                     + PROBE_GAP):
         raise ValueError("probe placement differs from the surrogate's frame")
-    return profile_features(batch), solve_fdtd(batch, nsteps, chunk, device), batch
+    if not on_device:
+        return profile_features(batch), solve_fdtd(batch, nsteps, chunk, device), batch
+    Y = torch.empty((n, OUT), dtype=torch.float32, device=device)
+    for s in range(0, n, chunk):
+        idx = np.arange(s, min(n, s + chunk))
+        Y[s:s + idx.size] = solve_fdtd_device(batch.subset(idx), nsteps, device=device)
+    return device_features(batch, device=device), Y, batch
 
 
 def train(model: FNO, inp: np.ndarray, tgt: np.ndarray, samples: int = 200_000, batch: int = 256,
@@ -505,38 +552,85 @@ class JudgedSurrogate:
     fraction of each request is re-solved by FDTD; a spot-checked profile whose
     error exceeds ``tol`` is replaced by its FDTD spectrum.  With ``gate`` =
     (layer_max, total_max), profiles selected by ``damping_gate`` skip the
-    network and are solved by FDTD directly."""
+    network and are solved by FDTD directly.
+
+    Everything stays on the device: the inputs are built there from the layer
+    tables (``device_features``), and the FDTD runs of the spot check (and of
+    the gated profiles) are enqueued on a second stream before the network
+    runs, so the two overlap; the replacement waits for both."""
 
     def __init__(self, model: FNO, check_frac: float = 0.01, tol: float = 0.01, nsteps: int = NSTEPS, seed: int = 0,
                  gate: tuple | None = None):
         self.model, self.check_frac, self.tol, self.nsteps = model, check_frac, tol, nsteps
         self.gate = gate
         self.rng = np.random.default_rng(seed)
+        self._side = None
 
     def __call__(self, batch: "B1.SlabBatch", inp: torch.Tensor | None = None):
+        """(pred [n][128] device tensor, info).  ``inp``: the batch's inputs
+        already on the device (built here otherwise)."""
+        dev = self.model.dev
         n = batch.nruns
         routed = damping_gate(batch, *self.gate) if self.gate else np.zeros(n, dtype=bool)
         served = np.nonzero(~routed)[0]
-        pred = np.zeros((n, OUT), dtype=np.float32)
+        routed_idx = np.nonzero(routed)[0]
+        k = max(1, int(round(self.check_frac * served.size))) if served.size else 0
+        idx = np.sort(self.rng.choice(served, size=min(k, served.size), replace=False)) if k else served[:0]
+        main = torch.cuda.current_stream(dev)
+        if self._side is None:
+            self._side = torch.cuda.Stream(device=dev)
+        side = self._side
+        side.wait_stream(main)
+        ref = fall = None
+        with torch.cuda.stream(side):  # the judge's FDTD, overlapping the network below
+            if idx.size:
+                ref = solve_fdtd_device(batch.subset(idx), self.nsteps, device=dev)
+            if routed_idx.size:
+                fall = solve_fdtd_device(batch.subset(routed_idx), self.nsteps, device=dev)
+        pred = torch.zeros((n, OUT), dtype=torch.float32, device=dev)
         if served.size:
+            sv = torch.as_tensor(served, device=dev)
             if inp is None:
-                x = torch.as_tensor(profile_features(batch, served, nbins=self.model.N)).to(self.model.dev)
+                x = device_features(batch, served, nbins=self.model.N, device=dev)
             else:
-                x = inp.index_select(0, torch.as_tensor(served, device=inp.device)).contiguous()
-            pred[served] = self.model.spectrum(x).cpu().numpy()
-        if routed.any():
-            pred[routed] = solve_fdtd(batch.subset(np.nonzero(routed)[0]), self.nsteps, device=self.model.dev)
-        info = {"routed": int(routed.sum()), "checked": 0, "fell_back": 0, "checked_idx": np.zeros(0, dtype=np.int64)}
-        if served.size:
-            k = max(1, int(round(self.check_frac * served.size)))
-            idx = np.sort(self.rng.choice(served, size=min(k, served.size), replace=False))
-            ref = solve_fdtd(batch.subset(idx), self.nsteps, device=self.model.dev)
-            err = rel_l2_spectrum(pred[idx], ref)
+                x = inp.index_select(0, sv).contiguous()
+            pred.index_copy_(0, sv, self.model.spectrum(x))
+        main.wait_stream(side)
+        for t in (ref, fall):
+            if t is not None:
+                t.record_stream(main)
+        info = {"routed": int(routed.sum()), "checked": int(idx.size), "fell_back": 0, "checked_idx": idx}
+        if routed_idx.size:
+            pred.index_copy_(0, torch.as_tensor(routed_idx, device=dev), fall)
+        if idx.size:
+            ci = torch.as_tensor(idx, device=dev)
+            err = rel_l2_spectrum_device(pred.index_select(0, ci), ref)
             bad = err > self.tol
-            pred[idx[bad]] = ref[bad]
-            info.update(checked=int(idx.size), check_err_median=float(np.median(err)),
-                        check_err_p90=float(np.quantile(err, 0.9)), fell_back=int(bad.sum()), checked_idx=idx)
+            pred.index_copy_(0, ci, torch.where(bad[:, None], ref, pred.index_select(0, ci)))
+            e = err.cpu().numpy()
+            info.update(check_err_median=float(np.median(e)), check_err_p90=float(np.quantile(e, 0.9)),
+                        fell_back=int((e > self.tol).sum()))
         return pred, info
+
+
+def time_served(model: FNO, batch: "B1.SlabBatch", check_frac: float = 0.01, tol: float = 0.01, reps: int = 1,
+                seed: int = 0) -> dict:
+    """Spectra per second of the judged server on ``batch`` (one request of
+    batch.nruns profiles): inputs built on the device, network, frame and
+    product, the 1% FDTD spot check overlapping them, replacements; timed
+    with CUDA events around whole requests (host work included)."""
+    judge = JudgedSurrogate(model, check_frac=check_frac, tol=tol, seed=seed)
+    judge(batch)  # warm-up: plans, buffers, module loads
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        pred, info = judge(batch)
+    e1.record(st)
+    torch.cuda.synchronize()
+    return {"spectra_per_s": reps * batch.nruns / (e0.elapsed_time(e1) / 1e3), "checked": info["checked"],
+            "fell_back": info["fell_back"], "pred": pred}
 
 
 def time_inference(model: FNO, n: int = 65536, chunk: int = 4096, reps: int = 2, seed: int = 0) -> float:
@@ -624,7 +718,7 @@ def main(argv=None) -> None:
         pred, info = judge(test, Xd)
         e1.record()
         torch.cuda.synchronize()
-        err = rel_l2_spectrum(pred, Yte)
+        err = rel_l2_spectrum(pred.cpu().numpy(), Yte)
         out[name] = {**summary(err), "routed": info["routed"], "checked": info["checked"],
                      "fell_back": info["fell_back"], "spectra_per_s": args.test / (e0.elapsed_time(e1) / 1e3)}
     e0.record()

@@ -172,7 +172,23 @@ def test_judge_replaces_bad_predictions(cuda_lib):
     pred, info = judge(batch)
     assert info["checked"] == 40 and info["fell_back"] >= 1
     ref = S.solve_fdtd(batch.subset(info["checked_idx"]), nsteps=2000)
-    assert np.all(S.rel_l2_spectrum(pred[info["checked_idx"]], ref) <= 0.01)
+    assert np.all(S.rel_l2_spectrum(pred.cpu().numpy()[info["checked_idx"]], ref) <= 0.01)
+
+
+def test_device_inputs_and_fdtd_spectra_match_host_forms(cuda_lib):
+    """The served path's device-built inputs equal profile_features bit for
+    bit (whole batch and a subset), and the device FDTD spectra equal the host
+    division to float32 rounding."""
+    from simulation_gb300 import batch1d as B1
+    from simulation_gb300 import surrogate as S
+    batch = B1.slab_batch(300, seed=12)
+    assert torch.equal(S.device_features(batch).cpu(), torch.from_numpy(S.profile_features(batch)))
+    idx = np.array([5, 17, 299, 0, 123])
+    assert torch.equal(S.device_features(batch, idx).cpu(), torch.from_numpy(S.profile_features(batch, idx)))
+    sub = batch.subset(np.arange(40))
+    d = S.solve_fdtd_device(sub, nsteps=1500).cpu().numpy()
+    h = S.solve_fdtd(sub, nsteps=1500)
+    np.testing.assert_allclose(d, h, rtol=1e-6, atol=1e-12)
 
 
 def test_trained_network_gains_over_baselines_and_fdtd(cuda_lib):
@@ -202,7 +218,7 @@ def test_trained_network_gains_over_baselines_and_fdtd(cuda_lib):
     # spectra end within 1%, and only a minority of profiles is re-solved
     judge = S.JudgedSurrogate(m, check_frac=0.01, tol=0.01, gate=(1.0, 6.0), seed=0)
     pred, info = judge(batch.subset(np.arange(ntr, ntr + 1024)), Xd)
-    e_gated = S.rel_l2_spectrum(pred, Yte)
+    e_gated = S.rel_l2_spectrum(pred.cpu().numpy(), Yte)
     assert info["routed"] <= 0.3 * 1024, info["routed"]
     assert np.mean(e_gated <= 0.01) >= np.mean(e_net <= 0.01) + 0.02, (np.mean(e_gated <= 0.01), np.mean(e_net <= 0.01))
     # throughput of the served path against the batched FDTD (default tuning) on the same distribution
