@@ -160,7 +160,7 @@ size_t fdtd2d_workspace_size(const fdtd2d_params* p, int steps_per_pass);
 /* fdtd2d_step_n: the program's time loop for t = t0+1 .. t0+nsteps, in the
  * reference's step order (fd2d/python/fd2d_3_4.py:268-277).  The core
  * D->source->E->H update is fused into one streaming kernel that keeps
- * `steps_per_pass` (1..4; 0 = library default) time steps in registers per
+ * `steps_per_pass` (1..4; 0 = library default: 2 below 2^21 cells, else 4) time steps in registers per
  * pass over HBM; `workspace` (fdtd2d_workspace_size bytes, 256-byte aligned)
  * holds the ping-pong copy of the evolving fields.  Results land in the
  * caller's arrays, bitwise equal to calling dfield/efield/hfield per step.

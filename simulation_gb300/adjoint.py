@@ -57,7 +57,10 @@ class AdjointProblem:
         if not (npml < self.src[0] and self.probe[0] < nx - npml):
             raise ValueError("source/probe inside the PML or outside the grid")
         self.sigma_box = sigma_box
-        self.sim = SimTM2D(nx, ny, pml=pmlparam(nx, ny, npml, grade, device), lossy=True,
+        # a box without conductivity runs the lossless E update: with nbz = 0
+        # the lossy one keeps iz = 0, and naz*(dz - 0) = naz*dz exactly, so the
+        # values are the same while iz and nbz are neither stored nor read
+        self.sim = SimTM2D(nx, ny, pml=pmlparam(nx, ny, npml, grade, device), lossy=sigma_box > 0,
                            source=PointSource(self.src[0], self.src[1], wave, src_kind), ns=ns, device=device,
                            check_finite=True)
         self.trace = torch.zeros(ns, dtype=torch.float32, device=self.device)
@@ -84,9 +87,10 @@ class AdjointProblem:
         e = eps_box.detach().to(self.device, torch.float64).reshape(bi, bj)
         nb = self.sigma_box * DT / EPS0
         self.sim.naz.fill_(1.0)
-        self.sim.nbz.zero_()
         self.sim.naz[i0:i0 + bi, j0:j0 + bj] = (1.0 / (e + nb)).float()
-        self.sim.nbz[i0:i0 + bi, j0:j0 + bj] = nb
+        if self.sim.nbz is not None:
+            self.sim.nbz.zero_()
+            self.sim.nbz[i0:i0 + bi, j0:j0 + bj] = nb
 
     # ------------------------------------------------------------ forward
     def _run(self, name: str, body) -> None:

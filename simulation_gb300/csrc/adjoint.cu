@@ -68,9 +68,15 @@ struct GlobalCells {
   __device__ __forceinline__ float lihy(int i, int j) const { return __ldg(a.adj.ihy + n(i, j)); }
 };
 
-template <class Cells>
+// UNIT: the tile's rows and columns all have unit PML coefficients and lie
+// inside the bounds tested below (k_adj_fused decides per tile).  With
+// fy2 = fx2 = 1 and fx1 = fy1 = 0 the general expressions reduce exactly
+// (1*x = x, fma(0, x, y) = y up to the sign of a zero), so both forms give
+// the same values.
+template <bool UNIT, class Cells>
 __device__ __forceinline__ float lam_cx(const AdjArgs& a, const Cells& c, int i, int j) {
   // adjoint of cx at (i, j) from hx', ihx' there (0 where H is not applied)
+  if constexpr (UNIT) return __fmaf_rn(0.5f, c.lhx(i, j), c.lihx(i, j));
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
   const float lhx = c.lhx(i, j);
   const float fy2 = __ldg(a.pml.fy2 + j);
@@ -78,8 +84,9 @@ __device__ __forceinline__ float lam_cx(const AdjArgs& a, const Cells& c, int i,
   return __fmaf_rn(__fmul_rn(0.5f, fy2), lhx, lihx_t);
 }
 
-template <class Cells>
+template <bool UNIT, class Cells>
 __device__ __forceinline__ float lam_cy(const AdjArgs& a, const Cells& c, int i, int j) {
+  if constexpr (UNIT) return __fmaf_rn(-0.5f, c.lhy(i, j), c.lihy(i, j));
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
   const float lhy = c.lhy(i, j);
   const float fx2 = __ldg(a.pml.fx2 + i);
@@ -93,15 +100,17 @@ __device__ __forceinline__ float lam_cy(const AdjArgs& a, const Cells& c, int i,
 // before the D update is undone.  With `own`, also writes L(iz) and adds the
 // cell's dJ/dnaz, dJ/dnbz (a cell computed only as a neighbour's halo does
 // neither).
-template <class Cells>
+template <bool UNIT = false, class Cells>
 __device__ __forceinline__ float adj_e(const AdjArgs& a, const Cells& c, int i, int j, bool own) {
   const size_t n = (size_t)i * a.ny + j;
   // forward recompute of dz' and ez at this cell (same formulas as the forward)
   float dzp = c.fdz(i, j);
-  if (i >= 1 && j >= 1)
+  if constexpr (UNIT)
+    dzp = d_update_unit(dzp, c.fhy(i, j), c.fhy(i - 1, j), c.fhx(i, j), c.fhx(i, j - 1));
+  else if (i >= 1 && j >= 1)
     dzp = d_update(dzp, c.fhy(i, j), c.fhy(i - 1, j), c.fhx(i, j), c.fhx(i, j - 1), __ldg(a.pml.gx3 + i),
                    __ldg(a.pml.gy3 + j), __ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j));
-  if (a.src_kind != FDTD_SRC_NONE && i == a.src_i && j == a.src_j) {
+  if (!UNIT && a.src_kind != FDTD_SRC_NONE && i == a.src_i && j == a.src_j) {
     const float v = __ldg(a.src_table + a.t - 1);
     dzp = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(dzp, v);
   }
@@ -110,7 +119,8 @@ __device__ __forceinline__ float adj_e(const AdjArgs& a, const Cells& c, int i, 
   const float naz = c.naz(i, j);
   const float ez = __fmul_rn(naz, diff);
   // adjoint of ez
-  float lez = lam_cx(a, c, i, j) - lam_cx(a, c, i, j - 1) + lam_cy(a, c, i, j) - lam_cy(a, c, i - 1, j);
+  float lez = lam_cx<UNIT>(a, c, i, j) - lam_cx<UNIT>(a, c, i, j - 1) + lam_cy<UNIT>(a, c, i, j) -
+              lam_cy<UNIT>(a, c, i - 1, j);
   if (i == a.probe_i && j == a.probe_j) lez = __fmaf_rn(a.probe_w, ez, lez);
   // E backward
   const float nbz = a.nbz ? c.nbz(i, j) : 0.f;
@@ -130,7 +140,9 @@ __device__ __forceinline__ float adj_e(const AdjArgs& a, const Cells& c, int i, 
 
 // cb*T at (i, j): the D adjoint flowing into the curl's H terms (0 where D is
 // not applied, or at a hard source whose dz' does not depend on the state)
+template <bool UNIT = false>
 __device__ __forceinline__ float dgrad(const AdjArgs& a, int i, int j, float T) {
+  if constexpr (UNIT) return __fmul_rn(0.5f, T);  // (gx2*gy2)*0.5 = 0.5; no source in the tile
   if (i < 1 || j < 1 || i >= a.nx || j >= a.ny) return 0.f;
   if (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j) return 0.f;
   const float cb = __fmul_rn(__fmul_rn(__ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j)), 0.5f);
@@ -140,26 +152,27 @@ __device__ __forceinline__ float dgrad(const AdjArgs& a, int i, int j, float T) 
 // D and H part of the reverse step at one cell, given T there (T) and at
 // the (i+1, j) and (i, j+1) neighbours (Ti, Tj): L(dz) = ca*T, L(hy) +=
 // cb*T - cb[i+1]*T[i+1], L(hx) += -cb*T + cb[j+1]*T[j+1], then H backward.
-template <class Cells>
+template <bool UNIT = false, class Cells>
 __device__ __forceinline__ void adj_dh(const AdjArgs& a, const Cells& c, int i, int j, float T, float Ti, float Tj) {
   const size_t n = (size_t)i * a.ny + j;
-  const bool hard_src = (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j);
+  const bool hard_src = !UNIT && (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j);
   float ldz;
-  if (hard_src) ldz = 0.f;
+  if (UNIT) ldz = T;  // (gx3*gy3)*T = 1*T
+  else if (hard_src) ldz = 0.f;
   else if (i >= 1 && j >= 1) ldz = __fmul_rn(__fmul_rn(__ldg(a.pml.gx3 + i), __ldg(a.pml.gy3 + j)), T);
   else ldz = T;
-  const float dg = dgrad(a, i, j, T);
-  const bool hm = (i <= a.nx - 2) && (j <= a.ny - 2);
+  const float dg = dgrad<UNIT>(a, i, j, T);
+  const bool hm = UNIT || ((i <= a.nx - 2) && (j <= a.ny - 2));
   float lhx = c.lhx(i, j), lhy = c.lhy(i, j), lihx = c.lihx(i, j), lihy = c.lihy(i, j);
-  if (hm) {
+  if (!UNIT && hm) {
     const float fy2 = __ldg(a.pml.fy2 + j), fx2 = __ldg(a.pml.fx2 + i);
     lihx = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, lihx);
     lihy = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, lihy);
     lhx = __fmul_rn(__ldg(a.pml.fy3 + j), lhx);
     lhy = __fmul_rn(__ldg(a.pml.fx3 + i), lhy);
   }
-  lhy = __fadd_rn(__fadd_rn(lhy, dg), -dgrad(a, i + 1, j, Ti));
-  lhx = __fadd_rn(__fsub_rn(lhx, dg), dgrad(a, i, j + 1, Tj));
+  lhy = __fadd_rn(__fadd_rn(lhy, dg), -dgrad<UNIT>(a, i + 1, j, Ti));
+  lhx = __fadd_rn(__fsub_rn(lhx, dg), dgrad<UNIT>(a, i, j + 1, Tj));
   a.out.dz[n] = ldz;
   a.out.hx[n] = lhx;
   a.out.hy[n] = lhy;
@@ -189,8 +202,9 @@ __global__ void k_adj_b(const AdjArgs a) {
 // copies every value the step reads for the tile, one row and one column of
 // halo below and right of it (whose T it needs) and one row and one column
 // above and left of that (their neighbours), into shared memory: twelve
-// fields over (kAdjTI+2) x 34 cells, all loads independent and issued
-// together.  Then it computes T on the tile and halo, then the D/H part for
+// fields over (kAdjTI+2) x 34 cells (widened to 40 for 16-byte copies), all
+// copies in flight together.  A tile whose cells all see unit PML
+// coefficients, no grid edge and no source takes the unit form.  Then it computes T on the tile and halo, then the D/H part for
 // the tile.  It reads the adjoints after step t (a.adj) and writes those
 // before it to other arrays (a.out): a halo cell's inputs belong to the
 // neighbouring tile, which must not have overwritten them.  Same per-cell
@@ -222,53 +236,103 @@ struct TileCells {
   __device__ __forceinline__ float lihy(int i, int j) const { return at(F_LIHY, i, j); }
 };
 
-__global__ void __launch_bounds__(kAdjTJ * kAdjThreadsY) k_adj_fused(const AdjArgs a) {
-  extern __shared__ float adj_smem[];
-  float (*tile)[kTileR][kTileC] = reinterpret_cast<float (*)[kTileR][kTileC]>(adj_smem);
-  float (*sT)[kAdjTJ + 1] = reinterpret_cast<float (*)[kAdjTJ + 1]>(adj_smem + F_COUNT * kTileR * kTileC);
-  const int j0 = blockIdx.x * kAdjTJ, i0 = blockIdx.y * kAdjTI;
-  const int tid = threadIdx.y * kAdjTJ + threadIdx.x;
-  const float* src[F_COUNT] = {a.fwd.dz, a.fwd.iz, a.fwd.hx, a.fwd.hy, a.naz, a.nbz,
-                               a.adj.dz, a.adj.iz, a.adj.hx, a.adj.hy, a.adj.ihx, a.adj.ihy};
-  static_assert(kTileR * kTileQ <= kAdjTJ * kAdjThreadsY, "one float4 group per thread and field");
-  if (tid < kTileR * kTileQ) {
-    const int r = tid / kTileQ, q = tid - r * kTileQ;
-    const int i = i0 - 1 + r, j = j0 - 4 + 4 * q;
-    const bool in = i >= 0 && i < a.nx && j >= 0 && j < a.ny;  // a group is wholly in or out
-    const size_t n = in ? (size_t)i * a.ny + j : 0;
-    float4 v[F_COUNT];
-#pragma unroll
-    for (int f = 0; f < F_COUNT; ++f)
-      v[f] = (in && src[f]) ? __ldg(reinterpret_cast<const float4*>(src[f] + n)) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int f = 0; f < F_COUNT; ++f) *reinterpret_cast<float4*>(&tile[f][r][4 * q]) = v[f];
-  }
-  __syncthreads();
-  const TileCells c{tile, i0, j0};
+// T on the tile and its halo into sT, then the D/H part on the tile
+template <bool UNIT>
+__device__ __forceinline__ void adj_tile(const AdjArgs& a, const TileCells& c, int i0, int j0,
+                                         float (*sT)[kAdjTJ + 1]) {
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int j = j0 + tx;
 #pragma unroll
   for (int k = 0; k < kAdjRows; ++k) {
     const int li = ty + kAdjThreadsY * k, i = i0 + li;
-    sT[li][tx] = (i < a.nx && j < a.ny) ? adj_e(a, c, i, j, true) : 0.f;
+    sT[li][tx] = (i < a.nx && j < a.ny) ? adj_e<UNIT>(a, c, i, j, true) : 0.f;
   }
   if (ty == 0) {  // halo row below the tile
     const int i = i0 + kAdjTI;
-    sT[kAdjTI][tx] = (i < a.nx && j < a.ny) ? adj_e(a, c, i, j, false) : 0.f;
+    sT[kAdjTI][tx] = (i < a.nx && j < a.ny) ? adj_e<UNIT>(a, c, i, j, false) : 0.f;
   } else if (ty == 1 && tx < kAdjTI) {  // halo column right of the tile
     const int i = i0 + tx, jj = j0 + kAdjTJ;
-    sT[tx][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, c, i, jj, false) : 0.f;
+    sT[tx][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e<UNIT>(a, c, i, jj, false) : 0.f;
   } else if (ty == 2 && tx == 0) {  // and their corner
     const int i = i0 + kAdjTI, jj = j0 + kAdjTJ;
-    sT[kAdjTI][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e(a, c, i, jj, false) : 0.f;
+    sT[kAdjTI][kAdjTJ] = (i < a.nx && jj < a.ny) ? adj_e<UNIT>(a, c, i, jj, false) : 0.f;
   }
   __syncthreads();
-  if (j >= a.ny) return;
+  if (j < a.ny) {
 #pragma unroll
-  for (int k = 0; k < kAdjRows; ++k) {
-    const int li = ty + kAdjThreadsY * k, i = i0 + li;
-    if (i < a.nx) adj_dh(a, c, i, j, sT[li][tx], sT[li + 1][tx], sT[li][tx + 1]);
+    for (int k = 0; k < kAdjRows; ++k) {
+      const int li = ty + kAdjThreadsY * k, i = i0 + li;
+      if (i < a.nx) adj_dh<UNIT>(a, c, i, j, sT[li][tx], sT[li + 1][tx], sT[li][tx + 1]);
+    }
   }
+}
+
+// cp.async of one 16-byte group into shared memory, zero-filled (nothing
+// read) where !ok; src must be a valid address either way
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, bool ok) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(ok ? 16u : 0u) : "memory");
+}
+
+// Stage tile k's twelve fields (rows i0-1 .. i0+TI, columns j0-4 .. j0+TJ+3)
+// into `tile` with one 16-byte cp.async per thread and field.
+__device__ __forceinline__ void stage_tile(const AdjArgs& a, float (*tile)[kTileR][kTileC], int i0, int j0, int tid) {
+  if (tid >= kTileR * kTileQ) return;
+  const float* src[F_COUNT] = {a.fwd.dz, a.fwd.iz, a.fwd.hx, a.fwd.hy, a.naz, a.nbz,
+                               a.adj.dz, a.adj.iz, a.adj.hx, a.adj.hy, a.adj.ihx, a.adj.ihy};
+  const int r = tid / kTileQ, q = tid - r * kTileQ;
+  const int i = i0 - 1 + r, j = j0 - 4 + 4 * q;
+  const bool in = i >= 0 && i < a.nx && j >= 0 && j < a.ny;  // a group is wholly in or out
+  const size_t n = in ? (size_t)i * a.ny + j : 0;
+#pragma unroll
+  for (int f = 0; f < F_COUNT; ++f) {
+    const bool ok = in && src[f] != nullptr;
+    cp_async16(&tile[f][r][4 * q], ok ? src[f] + n : a.naz, ok);
+  }
+}
+
+// Whether tile (i0, j0) takes the unit form: its rows i0-1 .. i0+TI and
+// columns j0-1 .. j0+TJ lie inside 0 .. n-2 with unit PML coefficients and
+// the source is not within a cell of it.  Each thread tests its share; the
+// caller combines them with __syncthreads_and.
+__device__ __forceinline__ bool tile_unit_part(const AdjArgs& a, int i0, int j0, int tid) {
+  if (tid < kTileR) {
+    const int i = i0 - 1 + tid;
+    return i >= 0 && i <= a.nx - 2 && __ldg(a.pml.fx1 + i) == 0.f && __ldg(a.pml.fx2 + i) == 1.f &&
+           __ldg(a.pml.fx3 + i) == 1.f && __ldg(a.pml.gx2 + i) == 1.f && __ldg(a.pml.gx3 + i) == 1.f;
+  }
+  if (tid >= 32 && tid < 32 + kAdjTJ + 2) {
+    const int j = j0 - 1 + (tid - 32);
+    return j >= 0 && j <= a.ny - 2 && __ldg(a.pml.fy1 + j) == 0.f && __ldg(a.pml.fy2 + j) == 1.f &&
+           __ldg(a.pml.fy3 + j) == 1.f && __ldg(a.pml.gy2 + j) == 1.f && __ldg(a.pml.gy3 + j) == 1.f;
+  }
+  if (tid == 96)
+    return a.src_kind == FDTD_SRC_NONE || a.src_i < i0 - 1 || a.src_i > i0 + kAdjTI + 1 || a.src_j < j0 - 1 ||
+           a.src_j > j0 + kAdjTJ + 1;
+  return true;
+}
+
+// One block per tile: stage it (one 16-byte cp.async per thread and field,
+// all in flight together), decide the form, compute.  (A persistent variant
+// that staged the next tile while computing the current one measured the
+// same 27 us per step at 1024^2, with twice the shared memory.)
+__global__ void __launch_bounds__(kAdjTJ * kAdjThreadsY) k_adj_fused(const AdjArgs a, int ntj) {
+  extern __shared__ float4 adj_smem4[];
+  float* adj_smem = reinterpret_cast<float*>(adj_smem4);
+  float (*tile)[kTileR][kTileC] = reinterpret_cast<float (*)[kTileR][kTileC]>(adj_smem);
+  float (*sT)[kAdjTJ + 1] = reinterpret_cast<float (*)[kAdjTJ + 1]>(adj_smem + F_COUNT * kTileR * kTileC);
+  const int tid = threadIdx.y * kAdjTJ + threadIdx.x;
+  const int i0 = (blockIdx.x / ntj) * kAdjTI, j0 = (blockIdx.x % ntj) * kAdjTJ;
+  stage_tile(a, tile, i0, j0, tid);
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  const bool part = tile_unit_part(a, i0, j0, tid);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  const bool unit = __syncthreads_and(part);  // also publishes the staged tile
+  const TileCells c{tile, i0, j0};
+  if (unit)
+    adj_tile<true>(a, c, i0, j0, sT);
+  else
+    adj_tile<false>(a, c, i0, j0, sT);
 }
 constexpr size_t kAdjSmem = (size_t)(F_COUNT * kTileR * kTileC + (kAdjTI + 1) * (kAdjTJ + 1)) * sizeof(float);
 
@@ -301,8 +365,8 @@ int launch_adjoint_fused(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd
   a.grad_naz = grad_naz;
   a.grad_nbz = grad_nbz;
   const dim3 blk(kAdjTJ, kAdjThreadsY);
-  const dim3 grd((p.ny + kAdjTJ - 1) / kAdjTJ, (p.nx + kAdjTI - 1) / kAdjTI);
-  k_adj_fused<<<grd, blk, kAdjSmem, st>>>(a);
+  const int ntj = (p.ny + kAdjTJ - 1) / kAdjTJ, nti = (p.nx + kAdjTI - 1) / kAdjTI;
+  k_adj_fused<<<ntj * nti, blk, kAdjSmem, st>>>(a, ntj);
   return fdtd_host::check_launch();
 }
 

@@ -36,7 +36,7 @@ namespace {
 
 using namespace fdtd;
 
-constexpr int kMaxK = 4;  // steps per fused pass
+constexpr int kMaxK = 4;  // most steps per fused pass (the record buffers of one pass)
 
 size_t slot(const fdtd2d_params* p) { return (((size_t)p->nx * p->ny * sizeof(float)) + 255) & ~(size_t)255; }
 int nfields(const fdtd2d_params* p) { return p->nbz ? 6 : 5; }  // dz, [iz], hx, hy, ihx, ihy
@@ -215,10 +215,11 @@ int run_forward(const fdtd2d_params* p0, const fdtd2d_adjoint_params* a, float* 
   for (int c = 0; c < L.ncp; ++c) {
     const int t_start = c * L.cp;
     const int len = std::min(L.cp, a->nsteps - t_start);
-    const int npass = (len + kMaxK - 1) / kMaxK;
+    const int kk = march_default_steps(p.nx, p.ny);
+    const int npass = (len + kk - 1) / kk;
     fdtd2d_fields in = ckpt(&p, L, c);
     for (int i = 0, t = t_start; i < npass; ++i) {
-      const int k = std::min(kMaxK, t_start + len - t);
+      const int k = std::min(kk, t_start + len - t);
       const fdtd2d_fields out = (i + 1 == npass) ? ckpt(&p, L, c + 1) : xbuf(&p, L, i % 2);
       if ((rc = launch_march(p, set_of(in), set_of(out), ez, t, k, nullptr, trace, st))) return rc;
       in = out;
@@ -239,7 +240,7 @@ int recompute(const fdtd2d_params* p, const Layout& L, int c, int len, int b, cu
   fdtd2d_fields in = ckpt(p, L, c);
   float* ez = at(L, L.ez);
   for (int t = t_start, i = 0; t < t_end; ++i) {
-    const int k = std::min(kMaxK, t_end - t);
+    const int k = std::min(march_default_steps(p->nx, p->ny), t_end - t);
     RecSet r[kMaxK];
     for (int s = 0; s < k; ++s) r[s] = rec(p, L, b, t - t_start + s);
     const fdtd2d_fields out = xbuf(p, L, i % 2);

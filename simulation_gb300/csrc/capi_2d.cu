@@ -191,7 +191,7 @@ int fdtd2d_step_n(const fdtd2d_params* p, fdtd2d_state* s, int t0, int nsteps, i
 
   // pass schedule with an even number of passes, so the last pass writes the
   // caller's arrays (split one pass if needed)
-  const int K = steps_per_pass == 0 ? march_max_steps_per_pass() : steps_per_pass;
+  const int K = steps_per_pass == 0 ? march_default_steps(p->nx, p->ny) : steps_per_pass;
   std::vector<int> sched;
   for (int rem = nsteps; rem > 0;) {
     const int k = rem < K ? rem : K;

@@ -36,6 +36,8 @@ int launch_march(const fdtd2d_params& p, const FieldSet& in, const FieldSet& out
                  int* status, float* probe_ez, cudaStream_t st);
 // columns a warp of the fused kernel owns (for workspace/grid sizing)
 int march_max_steps_per_pass();
+// steps per pass the library picks for a grid (steps_per_pass = 0)
+int march_default_steps(int nx, int ny);
 // A pass that also records the state after each of its steps (the adjoint's
 // recompute): rec[s] receives dz, iz, hx, hy after step t0+s+1, s < k.
 // Point source only, with PML (plain kernels, 64-column stripes).

@@ -108,7 +108,8 @@ def _stepwise_gradient(pr):
     lib = _lib.lib()
     s, p = pr.sim, pr.sim._p
     nx, ny, ns, cp = pr.nx, pr.ny, pr.ns, pr.cp
-    names = ("dz", "iz", "hx", "hy", "ihx", "ihy")
+    # iz only with a conducting box (the lossless update otherwise)
+    names = tuple(k for k in ("dz", "iz", "hx", "hy", "ihx", "ihy") if getattr(s, k) is not None)
     z = lambda *sh: torch.zeros(sh, dtype=torch.float32, device="cuda")  # noqa: E731
 
     def fields(buf):
@@ -122,13 +123,13 @@ def _stepwise_gradient(pr):
     p.probe_i, p.probe_j, p.probe_len = pr.probe[0], pr.probe[1], ns
     s._s.probe_ez = trace.data_ptr()
     ncp = -(-ns // cp)
-    ckpt = z(ncp, 6, nx, ny)
+    ckpt = z(ncp, len(names), nx, ny)
     for c in range(ncp):
         for k, name in enumerate(names):
             ckpt[c, k].copy_(getattr(s, name))
         s.step(min(cp, ns - c * cp))
     s._s.probe_ez = None
-    seg, adj, tmp, ez = z(cp, 6, nx, ny), z(6, nx, ny), z(nx, ny), z(nx, ny)
+    seg, adj, tmp, ez = z(cp, len(names), nx, ny), z(len(names), nx, ny), z(nx, ny), z(nx, ny)
     grad = z(pr.box[2], pr.box[3])
     box = _lib.Box2D(*pr.box)
     st = _lib.stream_ptr()
