@@ -454,7 +454,38 @@ def _bench_fd1d(st, reps: int = 20) -> dict:
                                "sample": "one config-1 run (ke=200, 1000 steps), float64 NumPy form of the reference"}
     except Exception as exc:  # reported, never fatal to the bench line
         res["cpu_baseline"] = {"error": f"{type(exc).__name__}: {exc}"}
+    try:  # and through the float32 C port of the reference's fd1d C loop (fd1d/clang/fd1d_1_3.c), one thread
+        res["cpu_baseline_c"] = _fd1d_config1_c()
+    except Exception as exc:
+        res["cpu_baseline_c"] = {"error": f"{type(exc).__name__}: {exc}"}
     return res
+
+
+def _fd1d_config1_c(budget_s: float = 2.0) -> dict:
+    """Config 1 (ke=200, 1000 steps, hard Gaussian source at k=5, ABC) on the
+    float32 C port, built for this host's CPU where possible; runs repeat from
+    zero fields until about ``budget_s`` seconds have passed."""
+    import numpy as np
+
+    from oracle import ccore
+    from oracle import fd1d as O1
+    lib, build = ccore.lib32_native(), "native"
+    if lib is None:
+        lib, build = ccore.lib32(), "portable"
+    kw = O1.program("config1")
+    nx = 200
+    cb = np.asarray(kw["cb"], dtype=np.float32)
+    table = np.array([O1.gaussian(t, 40, 12.0) for t in range(1, 1001)])
+    runs, el = 0, 0.0
+    while el < budget_s:
+        f = {k: np.zeros(nx, dtype=np.float32) for k in ("ex", "hy")}
+        f["bc"] = np.zeros(4, dtype=np.float32)
+        t0 = time.perf_counter()
+        ccore.fd1d_steps(lib, np.float32, nx, 0, 0, 1000, {"cb": cb}, 1, 5, table, True, f)
+        el += time.perf_counter() - t0
+        runs += 1
+    return {"us_per_run": el / runs * 1e6, "cores": 1, "kind": "port", "build": build, "host": host_cpu(),
+            "sample": f"{runs} config-1 runs (ke=200, 1000 steps) on the float32 C port of the reference's fd1d C loop"}
 
 
 def _bench_batch1d(st, nruns: int = 4096, autotune: bool = True, cpu: bool = False) -> dict:

@@ -440,8 +440,9 @@ int fdtd1d_hfield(const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t stream)
 /* fourier, fd1d/program/fd1d_2_2.py:65-71 (probes and optionally every cell). */
 int fdtd1d_fourier(int t, const fdtd1d_params* p, fdtd1d_state* s, fdtd_stream_t stream);
 /* fdtd1d_step_n: the program's time loop, t = t0+1 .. t0+nsteps, in one launch
- * (one thread-block cluster holds the whole line in registers; warp shuffles
- * and distributed shared memory carry the halos).  nx <= FDTD1D_MAX_FUSED_NX
+ * (a line of up to 512 cells is held by one warp, warp shuffles carrying the
+ * halos; a longer one by a thread block or cluster, with shared and distributed
+ * shared memory between warps and blocks).  nx <= FDTD1D_MAX_FUSED_NX
  * (8 blocks x 512 threads x 16 cells); longer lines use the per-function
  * entry points above.
  * Replaces fd1d/program/fd1d_1_3.py:53-62, fd1d/program/fd1d_2_2.py:138-142,

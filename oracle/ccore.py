@@ -86,6 +86,18 @@ def fd2d_steps(lib, real, nx, ny, t0, ns, pml, naz, nbz, src, src_table, f) -> N
                           _p(f.get("iz")), _p(f["hx"]), _p(f["hy"]), _p(f.get("ihx")), _p(f.get("ihy")))
 
 
+def fd1d_steps(lib, real, nx, form, t0, ns, co, src_kind, src_k, src_table, abc, f) -> None:
+    """Advance one 1D line in place: ``co`` maps ca/cb/nax/nbx/ncx/ndx to arrays
+    of dtype ``real`` (absent ones None), ``f`` maps ex/hy/dx/ix/sx/bc likewise;
+    ``src_table`` is float64, row t-1 for step t.  No DFT probes."""
+    st = np.ascontiguousarray(src_table, dtype=np.float64) if src_table is not None else np.zeros(1)
+    g = lambda k: _p(co.get(k))  # noqa: E731
+    h = lambda k: _p(f.get(k))  # noqa: E731
+    lib.oracle_fd1d_steps(nx, form, t0, ns, g("ca"), g("cb"), g("nax"), g("nbx"), g("ncx"), g("ndx"), src_kind,
+                          src_k, _p(st), int(abc), h("ex"), h("hy"), h("dx"), h("ix"), h("sx"), h("bc"), 0, None,
+                          None, 0, None, None, None)
+
+
 def fd1d_batch(lib, real, ke, layer_off, layer_start, layer_end, layer_ca, layer_cb, src_k, src_table, ns,
                dcos, dsin, probe_in, probe_out):
     """Spectra accumulators [nruns][4][nf] (re_in, im_in, re_out, im_out)."""

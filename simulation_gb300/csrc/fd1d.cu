@@ -5,7 +5,7 @@
 //
 // The fused kernel (fdtd1d_step_n) runs a whole time loop in ONE launch: one
 // thread-block cluster holds the line, each thread CPT consecutive cells in
-// registers.  Per time step it needs exactly two cluster-wide barriers:
+// registers (lines of up to 512 cells run in one warp instead, fd1d_warp.cuh).  Per time step it needs exactly two cluster-wide barriers:
 //   E stage  : ex (or dx -> ex) from hy, with the left neighbour's last hy
 //              read from shared memory (same block) or through distributed
 //              shared memory (previous block of the cluster); then the source,
@@ -22,6 +22,7 @@
 
 #include <algorithm>
 
+#include "fd1d_warp.cuh"
 #include "fdtd_common.cuh"
 
 namespace cg = cooperative_groups;
@@ -131,8 +132,8 @@ constexpr int RUN1D_MAX_THREADS = 1024;
 // block size limit per cells-per-thread, so the register budget grows with CPT
 __host__ __device__ constexpr int run1d_max_threads(int cpt) { return cpt <= 8 ? 1024 : 512; }
 
-template <int FORM, int CPT, bool CLUSTER, bool ONE_WARP>
-__global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d_run(const Run1DArgs a) {
+template <int FORM, int CPT, bool CLUSTER>
+__global__ void __launch_bounds__(run1d_max_threads(CPT)) k_fd1d_run(const Run1DArgs a) {
   const fdtd1d_params& p = a.p;
   const fdtd1d_state& s = a.s;
   __shared__ float x_first_ex[RUN1D_MAX_THREADS];
@@ -150,7 +151,6 @@ __global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d
   }
   auto sync_all = [&]() {
     if (CLUSTER) cg::this_cluster().sync();
-    else if (ONE_WARP) __syncwarp();
     else __syncthreads();
   };
   const int lane = tid & 31, w = tid >> 5, nw = T >> 5;
@@ -179,8 +179,8 @@ __global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d
     sxa[c] = (FORM == FDTD1D_FORM_DEBYE && in) ? s.sx[g] : 0.f;
   }
   // per-cell coefficients: in registers for the whole run when the register
-  // budget allows (one warp, or few cells per thread), else read from L1 each step
-  constexpr bool KREG = ONE_WARP || CPT <= 4;
+  // budget allows (few cells per thread), else read from L1 each step
+  constexpr bool KREG = CPT <= 4;
   float k0[CPT], k1[CPT], k2[CPT], k3[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; ++c) {
@@ -221,7 +221,10 @@ __global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d
     bc2 = s.bc[2];
     bc3 = s.bc[3];
   }
-  // probe DFT: thread f of the block that owns a probe cell accumulates it
+  // probe DFT: thread f of the block that owns a probe cell accumulates it in
+  // registers when nf <= threads per block, else the block's threads stride
+  // over f and accumulate in place in global memory
+  const bool pr_reg = p.nf <= T;
   float pr_r[FDTD1D_MAX_PROBES], pr_i[FDTD1D_MAX_PROBES];
 #pragma unroll
   for (int q = 0; q < FDTD1D_MAX_PROBES; ++q) {
@@ -231,8 +234,9 @@ __global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d
   unsigned my_probes = 0;  // probes owned by this block
   for (int q = 0; q < p.nprobe; ++q)
     if (p.probe_k[q] / (CPT * T) == rank) my_probes |= 1u << q;
-  if (tid < p.nf) {
-    for (int q = 0; q < p.nprobe; ++q)
+  if (pr_reg && tid < p.nf) {
+#pragma unroll
+    for (int q = 0; q < FDTD1D_MAX_PROBES; ++q)
       if (my_probes & (1u << q)) {
         pr_r[q] = s.r_pr[(size_t)q * p.nf + tid];
         pr_i[q] = s.i_pr[(size_t)q * p.nf + tid];
@@ -345,16 +349,32 @@ __global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d
       bc3 = bc2;
       bc2 = e_nm2;
     }
-    if (p.nf > 0 && tid < p.nf && my_probes) {
-      const float cf = __ldg(p.dft_cos + (size_t)(t - 1) * p.nf + tid);
-      const float sf = __ldg(p.dft_sin + (size_t)(t - 1) * p.nf + tid);
+    if (p.nf > 0 && my_probes) {
+      if (pr_reg) {
+        if (tid < p.nf) {
+          const float cf = __ldg(p.dft_cos + (size_t)(t - 1) * p.nf + tid);
+          const float sf = __ldg(p.dft_sin + (size_t)(t - 1) * p.nf + tid);
 #pragma unroll
-      for (int q = 0; q < FDTD1D_MAX_PROBES; ++q)
-        if (my_probes & (1u << q)) {
-          const float e = x_probe[q];
-          pr_r[q] = __fmaf_rn(cf, e, pr_r[q]);
-          pr_i[q] = __fmaf_rn(-sf, e, pr_i[q]);
+          for (int q = 0; q < FDTD1D_MAX_PROBES; ++q)
+            if (my_probes & (1u << q)) {
+              const float e = x_probe[q];
+              pr_r[q] = __fmaf_rn(cf, e, pr_r[q]);
+              pr_i[q] = __fmaf_rn(-sf, e, pr_i[q]);
+            }
         }
+      } else {
+        for (int f = tid; f < p.nf; f += T) {
+          const float cf = __ldg(p.dft_cos + (size_t)(t - 1) * p.nf + f);
+          const float sf = __ldg(p.dft_sin + (size_t)(t - 1) * p.nf + f);
+          for (int q = 0; q < p.nprobe; ++q)
+            if (my_probes & (1u << q)) {
+              const float e = x_probe[q];
+              const size_t m = (size_t)q * p.nf + f;
+              s.r_pr[m] = __fmaf_rn(cf, e, s.r_pr[m]);
+              s.i_pr[m] = __fmaf_rn(-sf, e, s.i_pr[m]);
+            }
+        }
+      }
     }
     float ex_right = next_first_ex;
     if (lane == 31) {
@@ -395,8 +415,9 @@ __global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d
     s.bc[2] = bc2;
     s.bc[3] = bc3;
   }
-  if (tid < p.nf) {
-    for (int q = 0; q < p.nprobe; ++q)
+  if (pr_reg && tid < p.nf) {
+#pragma unroll
+    for (int q = 0; q < FDTD1D_MAX_PROBES; ++q)
       if (my_probes & (1u << q)) {
         s.r_pr[(size_t)q * p.nf + tid] = pr_r[q];
         s.i_pr[(size_t)q * p.nf + tid] = pr_i[q];
@@ -407,9 +428,9 @@ __global__ void __launch_bounds__(ONE_WARP ? 32 : run1d_max_threads(CPT)) k_fd1d
 // ============================================================ launchers
 namespace {
 
-template <int FORM, int CPT, bool CLUSTER, bool ONE_WARP>
+template <int FORM, int CPT, bool CLUSTER>
 int launch_run_t(const Run1DArgs& a, int threads, int cluster, cudaStream_t st) {
-  auto kern = k_fd1d_run<FORM, CPT, CLUSTER, ONE_WARP>;
+  auto kern = k_fd1d_run<FORM, CPT, CLUSTER>;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(cluster, 1, 1);
   cfg.blockDim = dim3(threads, 1, 1);
@@ -434,18 +455,24 @@ int launch_run_t(const Run1DArgs& a, int threads, int cluster, cudaStream_t st) 
   return fdtd_host::check_launch();
 }
 
+// registers of the cluster variant (queried once per process)
 template <int FORM, int CPT>
 int regs_of() {
-  cudaFuncAttributes fa{};
-  if (cudaFuncGetAttributes(&fa, k_fd1d_run<FORM, CPT, true, false>) != cudaSuccess) return 255;
-  return fa.numRegs;
+  static const int regs = [] {
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, k_fd1d_run<FORM, CPT, true>) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return 255;
+    }
+    return fa.numRegs;
+  }();
+  return regs;
 }
 
 template <int FORM, int CPT>
 int launch_run_cpt(const Run1DArgs& a, int threads, int cluster, cudaStream_t st) {
-  if (cluster > 1) return launch_run_t<FORM, CPT, true, false>(a, threads, cluster, st);
-  if (threads == 32) return launch_run_t<FORM, CPT, false, true>(a, threads, cluster, st);
-  return launch_run_t<FORM, CPT, false, false>(a, threads, cluster, st);
+  if (cluster > 1) return launch_run_t<FORM, CPT, true>(a, threads, cluster, st);
+  return launch_run_t<FORM, CPT, false>(a, threads, cluster, st);
 }
 
 template <int FORM>
@@ -464,16 +491,6 @@ int launch_run_form(const Run1DArgs& a, cudaStream_t st) {
     t = (t / 32) * 32;
     return std::min(t, run1d_max_threads(cpt));
   };
-  // a line of up to 512 cells runs in ONE warp (no block barrier at all)
-  if (nx <= 32 * 16) {
-    const int cpt = nx <= 64 ? 2 : nx <= 128 ? 4 : nx <= 256 ? 8 : 16;
-    switch (cpt) {
-      case 2: return launch_run_cpt<FORM, 2>(a, 32, 1, st);
-      case 4: return launch_run_cpt<FORM, 4>(a, 32, 1, st);
-      case 8: return launch_run_cpt<FORM, 8>(a, 32, 1, st);
-      default: return launch_run_cpt<FORM, 16>(a, 32, 1, st);
-    }
-  }
   for (int pass = 0; pass < 3; ++pass) {
     const int limit_threads = pass == 0 ? 256 : RUN1D_MAX_THREADS;
     for (const Cand& c : cands) {
@@ -500,6 +517,8 @@ int launch_run_form(const Run1DArgs& a, cudaStream_t st) {
 }  // namespace
 
 int launch_fd1d_run(const fdtd1d_params& p, const fdtd1d_state& s, int t0, int nsteps, cudaStream_t st) {
+  // a line of up to 512 cells runs in ONE warp (no block barrier at all)
+  if (p.nx <= 32 * 16) return launch_fd1d_warp(p, s, t0, nsteps, st);
   Run1DArgs a{p, s, t0, nsteps};
   switch (p.form) {
     case FDTD1D_FORM_CB: return launch_run_form<FDTD1D_FORM_CB>(a, st);

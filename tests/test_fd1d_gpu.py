@@ -85,3 +85,72 @@ def test_fused_bitwise_sizes(cuda_lib, nx, form):
         x, y = getattr(a, k), getattr(b, k)
         if x is not None:
             assert torch.equal(x, y), f"{form} nx={nx}: {k} (max {float((x - y).abs().max()):.3e})"
+
+
+def _coeffs(nx, form):
+    from simulation_gb300 import fd1d as G
+    dt = 0.01 / 6e8
+    if form == "cb":
+        return {"cb": G.dielectric_cb(nx, 4.0)}
+    if form == "cacb":
+        ca, cb = G.dielectric_cacb(nx, dt, 4.0, 0.04)
+        return {"ca": ca, "cb": cb}
+    if form == "dform":
+        nax, nbx = G.dielectric_dform(nx, dt, 4.0, 0.04)
+        return {"nax": nax, "nbx": nbx}
+    nax, nbx, ncx, ndx = G.dielectric_debye(nx, dt, 2.0, 1e-9, 2.0, 0.01)
+    return {"nax": nax, "nbx": nbx, "ncx": ncx, "ndx": ndx}
+
+
+def _fused_vs_per_function(nx, form, ns, **kw):
+    from simulation_gb300 import fd1d as G
+    co = _coeffs(nx, form)
+    a, b = G.Sim1D(nx, form, **co, **kw), G.Sim1D(nx, form, **co, **kw)
+    a.step(ns)
+    b.step_per_function(ns)
+    torch.cuda.synchronize()
+    a.check()
+    for k in ("ex", "hy", "dx", "ix", "sx", "bc", "r_pt", "i_pt", "r_pr", "i_pr"):
+        x, y = getattr(a, k), getattr(b, k)
+        if x is not None:
+            assert torch.equal(x, y), f"{form} nx={nx} {kw}: {k} (max {float((x - y).abs().max()):.3e})"
+
+
+# one warp holds lines of up to 512 cells: 2, 4, 8 or 16 cells per lane; the
+# high-side ABC cell at the end of its lane (nx a multiple of the cells per
+# lane) or anywhere in it; the source at cell 0, at lane edges, at nx-1
+@pytest.mark.parametrize("nx,src_k", [(4, 0), (5, 4), (7, 1), (64, 63), (100, 8), (129, 4), (200, 5), (203, 31),
+                                      (256, 128), (257, 16), (480, 479), (511, 0), (512, 15)])
+@pytest.mark.parametrize("form", ["cb", "cacb", "dform", "debye"])
+def test_warp_kernel_bitwise(cuda_lib, nx, src_k, form):
+    hard = (nx + src_k) % 2 == 0
+    abc = nx % 3 != 2
+    _fused_vs_per_function(nx, form, 250, src_kind="hard" if hard else "soft", src_k=src_k,
+                           wave=("gauss", 20, 6.0), abc=abc, freq=[1e8, 3e8, 7e8],
+                           probes=(0, nx - 1, nx // 2), full_dft=nx % 2 == 1)
+
+
+@pytest.mark.parametrize("nx", [200, 201])
+def test_warp_kernel_no_source_no_dft(cuda_lib, nx):
+    from simulation_gb300 import fd1d as G
+    # a nonzero initial field and no source: the ABC alone drives the ends
+    co = _coeffs(nx, "cb")
+    a, b = G.Sim1D(nx, "cb", src_kind="none", **co), G.Sim1D(nx, "cb", src_kind="none", **co)
+    init = torch.sin(torch.arange(nx, dtype=torch.float32, device="cuda") * 0.1)
+    for s in (a, b):
+        s.ex.copy_(init)
+        s.hy.copy_(0.5 * init)
+    a.step(300)
+    b.step_per_function(300)
+    torch.cuda.synchronize()
+    for k in ("ex", "hy", "bc"):
+        assert torch.equal(getattr(a, k), getattr(b, k)), k
+
+
+@pytest.mark.parametrize("nx,nf", [(200, 40), (600, 200)])
+def test_probe_dft_more_frequencies_than_threads(cuda_lib, nx, nf):
+    """nf larger than the fused kernel's lanes (one warp) or threads per block:
+    the probe accumulators then live in global memory, same arithmetic."""
+    freq = np.linspace(5e7, 9e8, nf)
+    _fused_vs_per_function(nx, "dform", 120, src_kind="soft", src_k=3, wave=("gauss", 20, 6.0), freq=freq,
+                           probes=(1, nx // 3, nx - 2), full_dft=False)
