@@ -23,6 +23,8 @@
 //      writes L'(dz)+E terms to a temporary and L(iz) in place; gradients;
 //   B: D backward: L(dz) = ca*T, L(hy) += cb*T - cb[i+1]*T[i+1],
 //      L(hx) += -cb*T + cb[j+1]*T[j+1]; H backward for hx, hy, ihx, ihy.
+#include <type_traits>
+
 #include "fd2d_internal.cuh"
 
 namespace fdtd {
@@ -37,6 +39,7 @@ struct AdjArgs {
   int src_kind, src_i, src_j;
   const float* src_table;
   fdtd2d_fields fwd;  // state before step t
+  fdtd2d_fields fwd0;  // state before step t-1 (the two-step kernel only)
   fdtd2d_fields adj;  // adjoints after step t (read)
   fdtd2d_fields out;  // adjoints before step t (written; the same arrays as adj for the two-kernel step)
   float* tmp;
@@ -65,7 +68,17 @@ struct GlobalCells {
   __device__ __forceinline__ float lhx(int i, int j) const { return __ldg(a.adj.hx + n(i, j)); }
   __device__ __forceinline__ float lhy(int i, int j) const { return __ldg(a.adj.hy + n(i, j)); }
   __device__ __forceinline__ float lihx(int i, int j) const { return __ldg(a.adj.ihx + n(i, j)); }
-  __device__ __forceinline__ float lihy(int i, int j) const { return __ldg(a.adj.ihy + n(i, j)); }
+  __device__ __forceinline__ float lihy(int i, int j) const { return __ldg(a.adj.ihy + n(i, j)); }  // PML profile vectors (read through the cache)
+  __device__ __forceinline__ float fx1(int i) const { return __ldg(a.pml.fx1 + i); }
+  __device__ __forceinline__ float fx2(int i) const { return __ldg(a.pml.fx2 + i); }
+  __device__ __forceinline__ float fx3(int i) const { return __ldg(a.pml.fx3 + i); }
+  __device__ __forceinline__ float gx2(int i) const { return __ldg(a.pml.gx2 + i); }
+  __device__ __forceinline__ float gx3(int i) const { return __ldg(a.pml.gx3 + i); }
+  __device__ __forceinline__ float fy1(int j) const { return __ldg(a.pml.fy1 + j); }
+  __device__ __forceinline__ float fy2(int j) const { return __ldg(a.pml.fy2 + j); }
+  __device__ __forceinline__ float fy3(int j) const { return __ldg(a.pml.fy3 + j); }
+  __device__ __forceinline__ float gy2(int j) const { return __ldg(a.pml.gy2 + j); }
+  __device__ __forceinline__ float gy3(int j) const { return __ldg(a.pml.gy3 + j); }
 };
 
 // UNIT: the tile's rows and columns all have unit PML coefficients and lie
@@ -79,8 +92,8 @@ __device__ __forceinline__ float lam_cx(const AdjArgs& a, const Cells& c, int i,
   if constexpr (UNIT) return __fmaf_rn(0.5f, c.lhx(i, j), c.lihx(i, j));
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
   const float lhx = c.lhx(i, j);
-  const float fy2 = __ldg(a.pml.fy2 + j);
-  const float lihx_t = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, c.lihx(i, j));
+  const float fy2 = c.fy2(j);
+  const float lihx_t = __fmaf_rn(__fmul_rn(fy2, c.fx1(i)), lhx, c.lihx(i, j));
   return __fmaf_rn(__fmul_rn(0.5f, fy2), lhx, lihx_t);
 }
 
@@ -89,95 +102,126 @@ __device__ __forceinline__ float lam_cy(const AdjArgs& a, const Cells& c, int i,
   if constexpr (UNIT) return __fmaf_rn(-0.5f, c.lhy(i, j), c.lihy(i, j));
   if (i < 0 || j < 0 || i > a.nx - 2 || j > a.ny - 2) return 0.f;
   const float lhy = c.lhy(i, j);
-  const float fx2 = __ldg(a.pml.fx2 + i);
-  const float lihy_t = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, c.lihy(i, j));
+  const float fx2 = c.fx2(i);
+  const float lihy_t = __fmaf_rn(-__fmul_rn(fx2, c.fy1(j)), lhy, c.lihy(i, j));
   return __fmaf_rn(-__fmul_rn(0.5f, fx2), lhy, lihy_t);
 }
 
 // E part of the reverse step at one cell: recomputes dz' and ez from the
-// forward state, takes L(ez) from the H adjoints (+ the probe seed), runs the
-// E update backwards and returns T = L'(dz) + naz*L(ez~), the D adjoint
-// before the D update is undone.  With `own`, also writes L(iz) and adds the
-// cell's dJ/dnaz, dJ/dnbz (a cell computed only as a neighbour's halo does
-// neither).
-template <bool UNIT = false, class Cells>
-__device__ __forceinline__ float adj_e(const AdjArgs& a, const Cells& c, int i, int j, bool own) {
-  const size_t n = (size_t)i * a.ny + j;
+// forward state (before step t), takes L(ez) from the H adjoints (+ the probe
+// seed), runs the E update backwards.  T = L'(dz) + naz*L(ez~) is the D
+// adjoint before the D update is undone; liz the adjoint of iz before the
+// step; lezt, diff, ez and liz_in the terms of the cell's dJ/dnaz, dJ/dnbz.
+struct AdjE {
+  float T, liz, lezt, diff, ez, liz_in;
+};
+
+template <bool UNIT, class Cells>
+__device__ __forceinline__ AdjE adj_e_core(const AdjArgs& a, const Cells& c, int i, int j, int t) {
   // forward recompute of dz' and ez at this cell (same formulas as the forward)
   float dzp = c.fdz(i, j);
   if constexpr (UNIT)
     dzp = d_update_unit(dzp, c.fhy(i, j), c.fhy(i - 1, j), c.fhx(i, j), c.fhx(i, j - 1));
   else if (i >= 1 && j >= 1)
-    dzp = d_update(dzp, c.fhy(i, j), c.fhy(i - 1, j), c.fhx(i, j), c.fhx(i, j - 1), __ldg(a.pml.gx3 + i),
-                   __ldg(a.pml.gy3 + j), __ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j));
+    dzp = d_update(dzp, c.fhy(i, j), c.fhy(i - 1, j), c.fhx(i, j), c.fhx(i, j - 1), c.gx3(i),
+                   c.gy3(j), c.gx2(i), c.gy2(j));
   if (!UNIT && a.src_kind != FDTD_SRC_NONE && i == a.src_i && j == a.src_j) {
-    const float v = __ldg(a.src_table + a.t - 1);
+    const float v = __ldg(a.src_table + t - 1);
     dzp = (a.src_kind == FDTD_SRC_HARD) ? v : __fadd_rn(dzp, v);
   }
+  AdjE r;
   const float izv = a.nbz ? c.fiz(i, j) : 0.f;
-  const float diff = __fsub_rn(dzp, izv);
+  r.diff = __fsub_rn(dzp, izv);
   const float naz = c.naz(i, j);
-  const float ez = __fmul_rn(naz, diff);
+  r.ez = __fmul_rn(naz, r.diff);
   // adjoint of ez
   float lez = lam_cx<UNIT>(a, c, i, j) - lam_cx<UNIT>(a, c, i, j - 1) + lam_cy<UNIT>(a, c, i, j) -
               lam_cy<UNIT>(a, c, i - 1, j);
-  if (i == a.probe_i && j == a.probe_j) lez = __fmaf_rn(a.probe_w, ez, lez);
+  if (i == a.probe_i && j == a.probe_j) lez = __fmaf_rn(a.probe_w, r.ez, lez);
   // E backward
   const float nbz = a.nbz ? c.nbz(i, j) : 0.f;
-  const float liz = a.nbz ? c.liz(i, j) : 0.f;
-  const float lezt = __fmaf_rn(nbz, liz, lez);
-  if (own) {
-    if (a.nbz) a.out.iz[n] = __fmaf_rn(-naz, lezt, liz);
-    const int bi = i - a.box.i0, bj = j - a.box.j0;
-    if (a.grad_naz && bi >= 0 && bi < a.box.ni && bj >= 0 && bj < a.box.nj) {
-      const size_t b = (size_t)bi * a.box.nj + bj;
-      a.grad_naz[b] = __fmaf_rn(lezt, diff, a.grad_naz[b]);
-      if (a.grad_nbz) a.grad_nbz[b] = __fmaf_rn(liz, ez, a.grad_nbz[b]);
-    }
+  r.liz_in = a.nbz ? c.liz(i, j) : 0.f;
+  r.lezt = __fmaf_rn(nbz, r.liz_in, lez);
+  r.liz = __fmaf_rn(-naz, r.lezt, r.liz_in);
+  r.T = __fmaf_rn(naz, r.lezt, c.ldz(i, j));
+  return r;
+}
+
+// adds the cell's dJ/dnaz, dJ/dnbz of one step when it lies in the design box
+__device__ __forceinline__ void adj_grad(const AdjArgs& a, int i, int j, const AdjE& r) {
+  const int bi = i - a.box.i0, bj = j - a.box.j0;
+  if (a.grad_naz && bi >= 0 && bi < a.box.ni && bj >= 0 && bj < a.box.nj) {
+    const size_t b = (size_t)bi * a.box.nj + bj;
+    a.grad_naz[b] = __fmaf_rn(r.lezt, r.diff, a.grad_naz[b]);
+    if (a.grad_nbz) a.grad_nbz[b] = __fmaf_rn(r.liz_in, r.ez, a.grad_nbz[b]);
   }
-  return __fmaf_rn(naz, lezt, c.ldz(i, j));
+}
+
+// adj_e_core at step a.t; with `own`, also writes L(iz) and adds the cell's
+// gradient (a cell computed only as a neighbour's halo does neither)
+template <bool UNIT = false, class Cells>
+__device__ __forceinline__ float adj_e(const AdjArgs& a, const Cells& c, int i, int j, bool own) {
+  const AdjE r = adj_e_core<UNIT>(a, c, i, j, a.t);
+  if (own) {
+    if (a.nbz) a.out.iz[(size_t)i * a.ny + j] = r.liz;
+    adj_grad(a, i, j, r);
+  }
+  return r.T;
 }
 
 // cb*T at (i, j): the D adjoint flowing into the curl's H terms (0 where D is
 // not applied, or at a hard source whose dz' does not depend on the state)
-template <bool UNIT = false>
-__device__ __forceinline__ float dgrad(const AdjArgs& a, int i, int j, float T) {
+template <bool UNIT = false, class Cells>
+__device__ __forceinline__ float dgrad(const AdjArgs& a, const Cells& c, int i, int j, float T) {
   if constexpr (UNIT) return __fmul_rn(0.5f, T);  // (gx2*gy2)*0.5 = 0.5; no source in the tile
   if (i < 1 || j < 1 || i >= a.nx || j >= a.ny) return 0.f;
   if (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j) return 0.f;
-  const float cb = __fmul_rn(__fmul_rn(__ldg(a.pml.gx2 + i), __ldg(a.pml.gy2 + j)), 0.5f);
+  const float cb = __fmul_rn(__fmul_rn(c.gx2(i), c.gy2(j)), 0.5f);
   return __fmul_rn(cb, T);
 }
 
 // D and H part of the reverse step at one cell, given T there (T) and at
 // the (i+1, j) and (i, j+1) neighbours (Ti, Tj): L(dz) = ca*T, L(hy) +=
 // cb*T - cb[i+1]*T[i+1], L(hx) += -cb*T + cb[j+1]*T[j+1], then H backward.
-template <bool UNIT = false, class Cells>
-__device__ __forceinline__ void adj_dh(const AdjArgs& a, const Cells& c, int i, int j, float T, float Ti, float Tj) {
-  const size_t n = (size_t)i * a.ny + j;
+struct AdjDH {
+  float ldz, lhx, lhy, lihx, lihy;
+};
+
+template <bool UNIT, class Cells>
+__device__ __forceinline__ AdjDH adj_dh_core(const AdjArgs& a, const Cells& c, int i, int j, float T, float Ti,
+                                             float Tj) {
   const bool hard_src = !UNIT && (a.src_kind == FDTD_SRC_HARD && i == a.src_i && j == a.src_j);
-  float ldz;
-  if (UNIT) ldz = T;  // (gx3*gy3)*T = 1*T
-  else if (hard_src) ldz = 0.f;
-  else if (i >= 1 && j >= 1) ldz = __fmul_rn(__fmul_rn(__ldg(a.pml.gx3 + i), __ldg(a.pml.gy3 + j)), T);
-  else ldz = T;
-  const float dg = dgrad<UNIT>(a, i, j, T);
+  AdjDH r;
+  if (UNIT) r.ldz = T;  // (gx3*gy3)*T = 1*T
+  else if (hard_src) r.ldz = 0.f;
+  else if (i >= 1 && j >= 1) r.ldz = __fmul_rn(__fmul_rn(c.gx3(i), c.gy3(j)), T);
+  else r.ldz = T;
+  const float dg = dgrad<UNIT>(a, c, i, j, T);
   const bool hm = UNIT || ((i <= a.nx - 2) && (j <= a.ny - 2));
   float lhx = c.lhx(i, j), lhy = c.lhy(i, j), lihx = c.lihx(i, j), lihy = c.lihy(i, j);
   if (!UNIT && hm) {
-    const float fy2 = __ldg(a.pml.fy2 + j), fx2 = __ldg(a.pml.fx2 + i);
-    lihx = __fmaf_rn(__fmul_rn(fy2, __ldg(a.pml.fx1 + i)), lhx, lihx);
-    lihy = __fmaf_rn(-__fmul_rn(fx2, __ldg(a.pml.fy1 + j)), lhy, lihy);
-    lhx = __fmul_rn(__ldg(a.pml.fy3 + j), lhx);
-    lhy = __fmul_rn(__ldg(a.pml.fx3 + i), lhy);
+    const float fy2 = c.fy2(j), fx2 = c.fx2(i);
+    lihx = __fmaf_rn(__fmul_rn(fy2, c.fx1(i)), lhx, lihx);
+    lihy = __fmaf_rn(-__fmul_rn(fx2, c.fy1(j)), lhy, lihy);
+    lhx = __fmul_rn(c.fy3(j), lhx);
+    lhy = __fmul_rn(c.fx3(i), lhy);
   }
-  lhy = __fadd_rn(__fadd_rn(lhy, dg), -dgrad<UNIT>(a, i + 1, j, Ti));
-  lhx = __fadd_rn(__fsub_rn(lhx, dg), dgrad<UNIT>(a, i, j + 1, Tj));
-  a.out.dz[n] = ldz;
-  a.out.hx[n] = lhx;
-  a.out.hy[n] = lhy;
-  a.out.ihx[n] = lihx;
-  a.out.ihy[n] = lihy;
+  r.lhy = __fadd_rn(__fadd_rn(lhy, dg), -dgrad<UNIT>(a, c, i + 1, j, Ti));
+  r.lhx = __fadd_rn(__fsub_rn(lhx, dg), dgrad<UNIT>(a, c, i, j + 1, Tj));
+  r.lihx = lihx;
+  r.lihy = lihy;
+  return r;
+}
+
+template <bool UNIT = false, class Cells>
+__device__ __forceinline__ void adj_dh(const AdjArgs& a, const Cells& c, int i, int j, float T, float Ti, float Tj) {
+  const size_t n = (size_t)i * a.ny + j;
+  const AdjDH r = adj_dh_core<UNIT>(a, c, i, j, T, Ti, Tj);
+  a.out.dz[n] = r.ldz;
+  a.out.hx[n] = r.lhx;
+  a.out.hy[n] = r.lhy;
+  a.out.ihx[n] = r.lihx;
+  a.out.ihy[n] = r.lihy;
 }
 
 // Two-kernel form (in place, T through a full-grid temporary)
@@ -221,6 +265,7 @@ enum { F_FDZ, F_FIZ, F_FHX, F_FHY, F_NAZ, F_NBZ, F_LDZ, F_LIZ, F_LHX, F_LHY, F_L
 struct TileCells {
   const float (*t)[kTileR][kTileC];  // [field][row][column]
   int i0, j0;
+  const fdtd2d_pml* pml;
   __device__ __forceinline__ float at(int f, int i, int j) const { return t[f][i - i0 + 1][j - j0 + 4]; }
   __device__ __forceinline__ float fdz(int i, int j) const { return at(F_FDZ, i, j); }
   __device__ __forceinline__ float fiz(int i, int j) const { return at(F_FIZ, i, j); }
@@ -233,7 +278,16 @@ struct TileCells {
   __device__ __forceinline__ float lhx(int i, int j) const { return at(F_LHX, i, j); }
   __device__ __forceinline__ float lhy(int i, int j) const { return at(F_LHY, i, j); }
   __device__ __forceinline__ float lihx(int i, int j) const { return at(F_LIHX, i, j); }
-  __device__ __forceinline__ float lihy(int i, int j) const { return at(F_LIHY, i, j); }
+  __device__ __forceinline__ float lihy(int i, int j) const { return at(F_LIHY, i, j); }  __device__ __forceinline__ float fx1(int i) const { return __ldg(pml->fx1 + i); }
+  __device__ __forceinline__ float fx2(int i) const { return __ldg(pml->fx2 + i); }
+  __device__ __forceinline__ float fx3(int i) const { return __ldg(pml->fx3 + i); }
+  __device__ __forceinline__ float gx2(int i) const { return __ldg(pml->gx2 + i); }
+  __device__ __forceinline__ float gx3(int i) const { return __ldg(pml->gx3 + i); }
+  __device__ __forceinline__ float fy1(int j) const { return __ldg(pml->fy1 + j); }
+  __device__ __forceinline__ float fy2(int j) const { return __ldg(pml->fy2 + j); }
+  __device__ __forceinline__ float fy3(int j) const { return __ldg(pml->fy3 + j); }
+  __device__ __forceinline__ float gy2(int j) const { return __ldg(pml->gy2 + j); }
+  __device__ __forceinline__ float gy3(int j) const { return __ldg(pml->gy3 + j); }
 };
 
 // T on the tile and its halo into sT, then the D/H part on the tile
@@ -328,13 +382,271 @@ __global__ void __launch_bounds__(kAdjTJ * kAdjThreadsY) k_adj_fused(const AdjAr
   const bool part = tile_unit_part(a, i0, j0, tid);
   asm volatile("cp.async.wait_group 0;\n" ::: "memory");
   const bool unit = __syncthreads_and(part);  // also publishes the staged tile
-  const TileCells c{tile, i0, j0};
+  const TileCells c{tile, i0, j0, &a.pml};
   if (unit)
     adj_tile<true>(a, c, i0, j0, sT);
   else
     adj_tile<false>(a, c, i0, j0, sT);
 }
 constexpr size_t kAdjSmem = (size_t)(F_COUNT * kTileR * kTileC + (kAdjTI + 1) * (kAdjTJ + 1)) * sizeof(float);
+
+// ---------------------------------------------------------------- two steps
+// k_adj_fused2 undoes steps t and t-1 in one launch.  A block stages a kA2TI x
+// 32 tile with a two-cell halo (rows i0-2 .. i0+kA2TI+1, columns j0-4 .. j0+35
+// in 16-byte groups) of the adjoints after step t, both forward states (before
+// t and before t-1) and the material, then
+//   1. T of step t on the tile and a ring of one cell plus one more row below
+//      and column right (E1), and L(iz) of step t in place on the ring (R1);
+//   2. the D/H part of step t on R1, in place: the staged adjoints become the
+//      adjoints after step t-1 there;
+//   3. T of step t-1 on the tile plus one row below and one column right (E2);
+//   4. the D/H part of step t-1 on the tile, written out.
+// Every cell runs the same per-cell functions on the same operands as the
+// one-step kernels (a ring cell is the neighbouring tile's cell, computed
+// again), so the results are bitwise equal to two launches of k_adj_fused;
+// each tile cell adds its gradient terms of step t, then of step t-1.
+// Against two one-step launches it stages half the bytes, needs three block
+// barriers instead of four and launches once.
+// 8 x 32 tiles: 25.7 KB of shared memory (lossless box), 8 blocks per SM.  At
+// 1024^2 the reverse took 57.0 ms with 8-row tiles, 59.3 with 16, 65.5 with 24
+// and 72.2 with 32: occupancy pays more than the smaller halo share.
+constexpr int kA2TI = 8, kA2TJ = 32;  // kA2TI a multiple of 8, at most 60
+static_assert(kA2TI % 8 == 0 && kA2TI + 4 <= 64, "tile rows: phase 4 takes 8 rows per pass; unit test ranges");
+constexpr int kT2R = kA2TI + 4, kT2C = kA2TJ + 8, kT2Q = kT2C / 4;  // staged rows, columns, 16-byte groups
+constexpr int kE1R = kA2TI + 3, kE1C = kA2TJ + 3;                    // E1: rows i0-1 .., columns j0-1 ..
+constexpr int kR1R = kA2TI + 2, kR1C = kA2TJ + 2;                    // R1: the same origin
+constexpr int kE2R = kA2TI + 1, kE2C = kA2TJ + 1;                    // E2: rows i0 .., columns j0 ..
+
+template <bool LOSSY>
+struct A2F;
+template <>
+struct A2F<true> {
+  enum { F1DZ, F1IZ, F1HX, F1HY, F0DZ, F0IZ, F0HX, F0HY, NAZ, NBZ, LDZ, LIZ, LHX, LHY, LIHX, LIHY, COUNT };
+};
+template <>
+struct A2F<false> {
+  enum { F1DZ, F1HX, F1HY, F0DZ, F0HX, F0HY, NAZ, LDZ, LHX, LHY, LIHX, LIHY, COUNT, F1IZ = -1, F0IZ = -1,
+         NBZ = -1, LIZ = -1 };
+};
+
+// STEP 1: step t (state before t, adjoints after t); STEP 0: step t-1 (state
+// before t-1, the adjoints after t-1 that phase 2 left in the same arrays)
+// the PML profile vectors over the staged rows and columns, in shared memory
+enum { PX_FX1, PX_FX2, PX_FX3, PX_GX2, PX_GX3, PX_COUNT };
+enum { PY_FY1, PY_FY2, PY_FY3, PY_GY2, PY_GY3, PY_COUNT };
+constexpr int kPYC = kA2TJ + 4;  // columns j0-2 .. j0+TJ+1
+
+template <bool LOSSY, int STEP>
+struct Tile2Cells {
+  using F = A2F<LOSSY>;
+  float (*t)[kT2R][kT2C];
+  int i0, j0;
+  const float (*px)[kT2R];  // [vector][row i - i0 + 2]
+  const float (*py)[kPYC];  // [vector][column j - j0 + 2]
+  __device__ __forceinline__ float fx1(int i) const { return px[PX_FX1][i - i0 + 2]; }
+  __device__ __forceinline__ float fx2(int i) const { return px[PX_FX2][i - i0 + 2]; }
+  __device__ __forceinline__ float fx3(int i) const { return px[PX_FX3][i - i0 + 2]; }
+  __device__ __forceinline__ float gx2(int i) const { return px[PX_GX2][i - i0 + 2]; }
+  __device__ __forceinline__ float gx3(int i) const { return px[PX_GX3][i - i0 + 2]; }
+  __device__ __forceinline__ float fy1(int j) const { return py[PY_FY1][j - j0 + 2]; }
+  __device__ __forceinline__ float fy2(int j) const { return py[PY_FY2][j - j0 + 2]; }
+  __device__ __forceinline__ float fy3(int j) const { return py[PY_FY3][j - j0 + 2]; }
+  __device__ __forceinline__ float gy2(int j) const { return py[PY_GY2][j - j0 + 2]; }
+  __device__ __forceinline__ float gy3(int j) const { return py[PY_GY3][j - j0 + 2]; }
+  __device__ __forceinline__ float at(int f, int i, int j) const { return t[f][i - i0 + 2][j - j0 + 4]; }
+  __device__ __forceinline__ float fdz(int i, int j) const { return at(STEP ? F::F1DZ : F::F0DZ, i, j); }
+  __device__ __forceinline__ float fiz(int i, int j) const {
+    return LOSSY ? at(STEP ? F::F1IZ : F::F0IZ, i, j) : 0.f;
+  }
+  __device__ __forceinline__ float fhx(int i, int j) const { return at(STEP ? F::F1HX : F::F0HX, i, j); }
+  __device__ __forceinline__ float fhy(int i, int j) const { return at(STEP ? F::F1HY : F::F0HY, i, j); }
+  __device__ __forceinline__ float naz(int i, int j) const { return at(F::NAZ, i, j); }
+  __device__ __forceinline__ float nbz(int i, int j) const { return LOSSY ? at(F::NBZ, i, j) : 0.f; }
+  __device__ __forceinline__ float ldz(int i, int j) const { return at(F::LDZ, i, j); }
+  __device__ __forceinline__ float liz(int i, int j) const { return LOSSY ? at(F::LIZ, i, j) : 0.f; }
+  __device__ __forceinline__ float lhx(int i, int j) const { return at(F::LHX, i, j); }
+  __device__ __forceinline__ float lhy(int i, int j) const { return at(F::LHY, i, j); }
+  __device__ __forceinline__ float lihx(int i, int j) const { return at(F::LIHX, i, j); }
+  __device__ __forceinline__ float lihy(int i, int j) const { return at(F::LIHY, i, j); }
+};
+
+template <bool LOSSY>
+__device__ __forceinline__ void stage_tile2(const AdjArgs& a, float (*tile)[kT2R][kT2C], int i0, int j0, int tid) {
+  constexpr int N = A2F<LOSSY>::COUNT;
+  const float* src[16];
+  if (LOSSY) {
+    const float* s16[16] = {a.fwd.dz,  a.fwd.iz, a.fwd.hx, a.fwd.hy, a.fwd0.dz, a.fwd0.iz, a.fwd0.hx, a.fwd0.hy,
+                            a.naz,     a.nbz,    a.adj.dz, a.adj.iz, a.adj.hx,  a.adj.hy,  a.adj.ihx, a.adj.ihy};
+    for (int f = 0; f < 16; ++f) src[f] = s16[f];
+  } else {
+    const float* s12[12] = {a.fwd.dz, a.fwd.hx, a.fwd.hy, a.fwd0.dz, a.fwd0.hx, a.fwd0.hy,
+                            a.naz,    a.adj.dz, a.adj.hx, a.adj.hy,  a.adj.ihx, a.adj.ihy};
+    for (int f = 0; f < 12; ++f) src[f] = s12[f];
+  }
+  for (int g = tid; g < kT2R * kT2Q; g += kA2TJ * 8) {
+    const int r = g / kT2Q, q = g - r * kT2Q;
+    const int i = i0 - 2 + r, j = j0 - 4 + 4 * q;
+    const bool in = i >= 0 && i < a.nx && j >= 0 && j < a.ny;  // a group is wholly in or out (ny % 4 == 0)
+    const size_t n = in ? (size_t)i * a.ny + j : 0;
+#pragma unroll
+    for (int f = 0; f < N; ++f) cp_async16(&tile[f][r][4 * q], in ? src[f] + n : a.naz, in);
+  }
+}
+
+// Copies the PML vectors of the staged rows (i0-2 .. i0+TI+1) and columns
+// (j0-2 .. j0+TJ+1) into px/py (0 outside the grid, where no cell reads
+// them) and tells whether this thread's share allows the unit form: those
+// rows and columns inside 0 .. n-2 with unit PML coefficients, and no source
+// near the tile.
+__device__ __forceinline__ bool tile2_unit_part(const AdjArgs& a, int i0, int j0, int tid, float (*px)[kT2R],
+                                                float (*py)[kPYC]) {
+  if (tid < kT2R) {
+    const int i = i0 - 2 + tid;
+    const bool in = i >= 0 && i < a.nx;
+    const float f1 = in ? __ldg(a.pml.fx1 + i) : 0.f, f2 = in ? __ldg(a.pml.fx2 + i) : 0.f;
+    const float f3 = in ? __ldg(a.pml.fx3 + i) : 0.f, g2 = in ? __ldg(a.pml.gx2 + i) : 0.f;
+    const float g3 = in ? __ldg(a.pml.gx3 + i) : 0.f;
+    px[PX_FX1][tid] = f1;
+    px[PX_FX2][tid] = f2;
+    px[PX_FX3][tid] = f3;
+    px[PX_GX2][tid] = g2;
+    px[PX_GX3][tid] = g3;
+    return i >= 0 && i <= a.nx - 2 && f1 == 0.f && f2 == 1.f && f3 == 1.f && g2 == 1.f && g3 == 1.f;
+  }
+  if (tid >= 64 && tid < 64 + kPYC) {
+    const int c = tid - 64, j = j0 - 2 + c;
+    const bool in = j >= 0 && j < a.ny;
+    const float f1 = in ? __ldg(a.pml.fy1 + j) : 0.f, f2 = in ? __ldg(a.pml.fy2 + j) : 0.f;
+    const float f3 = in ? __ldg(a.pml.fy3 + j) : 0.f, g2 = in ? __ldg(a.pml.gy2 + j) : 0.f;
+    const float g3 = in ? __ldg(a.pml.gy3 + j) : 0.f;
+    py[PY_FY1][c] = f1;
+    py[PY_FY2][c] = f2;
+    py[PY_FY3][c] = f3;
+    py[PY_GY2][c] = g2;
+    py[PY_GY3][c] = g3;
+    return j >= 0 && j <= a.ny - 2 && f1 == 0.f && f2 == 1.f && f3 == 1.f && g2 == 1.f && g3 == 1.f;
+  }
+  if (tid == 128)
+    return a.src_kind == FDTD_SRC_NONE || a.src_i < i0 - 2 || a.src_i > i0 + kA2TI + 2 || a.src_j < j0 - 2 ||
+           a.src_j > j0 + kA2TJ + 2;
+  return true;
+}
+
+template <bool UNIT, bool LOSSY>
+__device__ __forceinline__ void adj_tile2(const AdjArgs& a, float (*tile)[kT2R][kT2C], int i0, int j0, int tid,
+                                          float (*s1)[kE1C], float (*s2)[kE2C], const float (*px)[kT2R],
+                                          const float (*py)[kPYC]) {
+  using F = A2F<LOSSY>;
+  const Tile2Cells<LOSSY, 1> c1{tile, i0, j0, px, py};
+  const Tile2Cells<LOSSY, 0> c0{tile, i0, j0, px, py};
+  auto in_grid = [&](int i, int j) { return i >= 0 && i < a.nx && j >= 0 && j < a.ny; };
+  // A region of R rows x C columns (C > 32) is covered row by row: warp w
+  // takes rows w, w+8, ..., its lanes the first 32 columns (consecutive
+  // shared-memory words, no bank conflict); the other C-32 columns go to the
+  // threads of the warps from R % 8 on, which have one row fewer.
+  const int lane = threadIdx.x, w = threadIdx.y, tid_ = w * 32 + lane;
+  auto cover = [&](auto R, auto C, auto&& cell) {
+    constexpr int kR = decltype(R)::value, kC = decltype(C)::value, kX = kC - 32;
+    for (int li = w; li < kR; li += 8) cell(li, lane);
+    for (int k = (tid_ + 256 - (kR % 8) * 32) % 256; k < kR * kX; k += 256) {
+      const int li = k / kX;
+      cell(li, 32 + (k - li * kX));
+    }
+  };
+  // 1. step t: T on E1, L(iz) in place on R1, gradient terms of the tile
+  cover(std::integral_constant<int, kE1R>{}, std::integral_constant<int, kE1C>{}, [&](int li, int lj) {
+    const int i = i0 - 1 + li, j = j0 - 1 + lj;
+    float T = 0.f;
+    if (UNIT || in_grid(i, j)) {
+      const AdjE r = adj_e_core<UNIT>(a, c1, i, j, a.t);
+      T = r.T;
+      if (LOSSY && li < kR1R && lj < kR1C) tile[F::LIZ][li + 1][lj + 3] = r.liz;
+      if (li >= 1 && li <= kA2TI && lj >= 1 && lj <= kA2TJ) adj_grad(a, i, j, r);
+    }
+    s1[li][lj] = T;
+  });
+  __syncthreads();
+  // 2. step t: D/H on R1, in place
+  cover(std::integral_constant<int, kR1R>{}, std::integral_constant<int, kR1C>{}, [&](int li, int lj) {
+    const int i = i0 - 1 + li, j = j0 - 1 + lj;
+    if (UNIT || in_grid(i, j)) {
+      const AdjDH r = adj_dh_core<UNIT>(a, c1, i, j, s1[li][lj], s1[li + 1][lj], s1[li][lj + 1]);
+      tile[F::LDZ][li + 1][lj + 3] = r.ldz;
+      tile[F::LHX][li + 1][lj + 3] = r.lhx;
+      tile[F::LHY][li + 1][lj + 3] = r.lhy;
+      tile[F::LIHX][li + 1][lj + 3] = r.lihx;
+      tile[F::LIHY][li + 1][lj + 3] = r.lihy;
+    }
+  });
+  __syncthreads();
+  // 3. step t-1: T on E2; L(iz) and gradient terms of the tile
+  cover(std::integral_constant<int, kE2R>{}, std::integral_constant<int, kE2C>{}, [&](int li, int lj) {
+    const int i = i0 + li, j = j0 + lj;
+    float T = 0.f;
+    if (UNIT || in_grid(i, j)) {
+      const AdjE r = adj_e_core<UNIT>(a, c0, i, j, a.t - 1);
+      T = r.T;
+      if (li < kA2TI && lj < kA2TJ) {
+        if (LOSSY) a.out.iz[(size_t)i * a.ny + j] = r.liz;
+        adj_grad(a, i, j, r);
+      }
+    }
+    s2[li][lj] = T;
+  });
+  __syncthreads();
+  // 4. step t-1: D/H on the tile
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int j = j0 + tx;
+  if (j < a.ny) {
+#pragma unroll
+    for (int k = 0; k < kA2TI / 8; ++k) {
+      const int li = ty + 8 * k, i = i0 + li;
+      if (i < a.nx) adj_dh<UNIT>(a, c0, i, j, s2[li][tx], s2[li + 1][tx], s2[li][tx + 1]);
+    }
+  }
+}
+
+template <bool LOSSY>
+constexpr size_t adj2_smem() {
+  return (size_t)(A2F<LOSSY>::COUNT * kT2R * kT2C + kE1R * kE1C + kE2R * kE2C + PX_COUNT * kT2R + PY_COUNT * kPYC) *
+         sizeof(float);
+}
+
+template <bool LOSSY>
+__global__ void __launch_bounds__(kA2TJ * 8) k_adj_fused2(const AdjArgs a, int ntj) {
+  extern __shared__ float4 adj2_smem4[];
+  float* sm = reinterpret_cast<float*>(adj2_smem4);
+  float (*tile)[kT2R][kT2C] = reinterpret_cast<float (*)[kT2R][kT2C]>(sm);
+  float (*s1)[kE1C] = reinterpret_cast<float (*)[kE1C]>(sm + A2F<LOSSY>::COUNT * kT2R * kT2C);
+  float* rest = sm + A2F<LOSSY>::COUNT * kT2R * kT2C + kE1R * kE1C;
+  float (*s2)[kE2C] = reinterpret_cast<float (*)[kE2C]>(rest);
+  float (*px)[kT2R] = reinterpret_cast<float (*)[kT2R]>(rest + kE2R * kE2C);
+  float (*py)[kPYC] = reinterpret_cast<float (*)[kPYC]>(rest + kE2R * kE2C + PX_COUNT * kT2R);
+  const int tid = threadIdx.y * kA2TJ + threadIdx.x;
+  const int i0 = (blockIdx.x / ntj) * kA2TI, j0 = (blockIdx.x % ntj) * kA2TJ;
+  stage_tile2<LOSSY>(a, tile, i0, j0, tid);
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  const bool part = tile2_unit_part(a, i0, j0, tid, px, py);
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  const bool unit = __syncthreads_and(part);  // also publishes the staged tile and vectors
+  if (unit)
+    adj_tile2<true, LOSSY>(a, tile, i0, j0, tid, s1, s2, px, py);
+  else
+    adj_tile2<false, LOSSY>(a, tile, i0, j0, tid, s1, s2, px, py);
+}
+
+template <bool LOSSY>
+int launch_adj2(const AdjArgs& a, cudaStream_t st) {
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(k_adj_fused2<LOSSY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)adj2_smem<LOSSY>());
+  if (attr != cudaSuccess) {
+    fdtd_host::note_cuda_error(attr);
+    return FDTD_ERR_CUDA;
+  }
+  const int ntj = (a.ny + kA2TJ - 1) / kA2TJ, nti = (a.nx + kA2TI - 1) / kA2TI;
+  k_adj_fused2<LOSSY><<<ntj * nti, dim3(kA2TJ, 8), adj2_smem<LOSSY>(), st>>>(a, ntj);
+  return fdtd_host::check_launch();
+}
 
 }  // namespace
 
@@ -368,6 +680,36 @@ int launch_adjoint_fused(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd
   const int ntj = (p.ny + kAdjTJ - 1) / kAdjTJ, nti = (p.nx + kAdjTI - 1) / kAdjTI;
   k_adj_fused<<<ntj * nti, blk, kAdjSmem, st>>>(a, ntj);
   return fdtd_host::check_launch();
+}
+
+// Steps t and t-1 in one launch (k_adj_fused2): adjoints after step t from
+// adj_in, before step t-1 to adj_out; fwd1/fwd0 = the states before t / t-1.
+int launch_adjoint_fused2(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd1, const fdtd2d_fields& fwd0,
+                          const fdtd2d_fields& adj_in, const fdtd2d_fields& adj_out, int probe_i, int probe_j,
+                          float probe_w, const fdtd2d_box& box, float* grad_naz, float* grad_nbz, cudaStream_t st) {
+  AdjArgs a{};
+  a.nx = p.nx;
+  a.ny = p.ny;
+  a.t = t;
+  a.pml = p.pml;
+  a.naz = p.naz;
+  a.nbz = p.nbz;
+  a.src_kind = p.src.kind;
+  a.src_i = p.src.i;
+  a.src_j = p.src.j;
+  a.src_table = p.src.table;
+  a.fwd = fwd1;
+  a.fwd0 = fwd0;
+  a.adj = adj_in;
+  a.out = adj_out;
+  a.tmp = nullptr;
+  a.probe_i = probe_i;
+  a.probe_j = probe_j;
+  a.probe_w = probe_w;
+  a.box = box;
+  a.grad_naz = grad_naz;
+  a.grad_nbz = grad_nbz;
+  return p.nbz ? launch_adj2<true>(a, st) : launch_adj2<false>(a, st);
 }
 
 }  // namespace fdtd

@@ -15,7 +15,8 @@
 //             dz, iz, hx, hy after each of its steps), on a second stream,
 //             one segment ahead of the sweep (two record buffers, events
 //             order their reuse); the sweep runs one fused reverse kernel per
-//             step, the adjoint fields ping-ponging between two sets.
+//             two steps (one step for an odd segment's first), the adjoint
+//             fields ping-ponging between two sets.
 // Results do not depend on the checkpoint interval or on the overlap: every
 // recorded state is bitwise the forward's, and each reverse step does the
 // same per-cell arithmetic (fdtd2d_adjoint_step's two kernels give the same
@@ -30,6 +31,9 @@ namespace fdtd {
 int launch_adjoint_fused(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd, const fdtd2d_fields& adj_in,
                          const fdtd2d_fields& adj_out, int probe_i, int probe_j, float probe_w,
                          const fdtd2d_box& box, float* grad_naz, float* grad_nbz, cudaStream_t st);
+int launch_adjoint_fused2(const fdtd2d_params& p, int t, const fdtd2d_fields& fwd1, const fdtd2d_fields& fwd0,
+                          const fdtd2d_fields& adj_in, const fdtd2d_fields& adj_out, int probe_i, int probe_j,
+                          float probe_w, const fdtd2d_box& box, float* grad_naz, float* grad_nbz, cudaStream_t st);
 }  // namespace fdtd
 
 namespace {
@@ -283,17 +287,21 @@ int run_reverse(const fdtd2d_params* p, const fdtd2d_adjoint_params* a, float* g
     }
     if ((rc = cuda_rc(cudaStreamWaitEvent(main, side->ready[b], 0)))) return rc;
     const int t_start = c * L.cp, len = seg_len(c);
-    for (int t = t_start + len; t > t_start; --t) {
-      fdtd2d_fields fwd;
-      if (t == t_start + 1) {
-        fwd = ckpt(p, L, c);
-      } else {
-        const RecSet r = rec(p, L, b, t - t_start - 2);
-        fwd = fdtd2d_fields{r.dz, r.iz, r.hx, r.hy, nullptr, nullptr};
-      }
-      if ((rc = launch_adjoint_fused(*p, t, fwd, adjbuf(p, L, cur), adjbuf(p, L, 1 - cur), a->probe_i, a->probe_j,
-                                     a->probe_weight, a->box, grad_naz, grad_nbz, main)))
-        return rc;
+    // the state before step t: the checkpoint, or a recorded state
+    auto fwd_of = [&](int t) {
+      if (t == t_start + 1) return ckpt(p, L, c);
+      const RecSet r = rec(p, L, b, t - t_start - 2);
+      return fdtd2d_fields{r.dz, r.iz, r.hx, r.hy, nullptr, nullptr};
+    };
+    // two steps per launch; an odd segment's first step alone
+    for (int t = t_start + len; t > t_start; t -= 2) {
+      if (t - 1 > t_start)
+        rc = launch_adjoint_fused2(*p, t, fwd_of(t), fwd_of(t - 1), adjbuf(p, L, cur), adjbuf(p, L, 1 - cur),
+                                   a->probe_i, a->probe_j, a->probe_weight, a->box, grad_naz, grad_nbz, main);
+      else
+        rc = launch_adjoint_fused(*p, t, fwd_of(t), adjbuf(p, L, cur), adjbuf(p, L, 1 - cur), a->probe_i,
+                                  a->probe_j, a->probe_weight, a->box, grad_naz, grad_nbz, main);
+      if (rc) return rc;
       cur = 1 - cur;
     }
     if ((rc = cuda_rc(cudaEventRecord(side->free_[b], main)))) return rc;

@@ -98,7 +98,7 @@ def test_adjoint_vs_central_fd_config4(cuda_lib):
     assert rl2 <= 1e-3, f"rel-L2 {rl2:.3e}"
 
 
-def _stepwise_gradient(pr):
+def _stepwise_gradient(pr, with_nbz=False):
     """dJ/dnaz by the reference-granularity entry points: the forward as
     fdtd2d_step_n calls per checkpoint segment, each segment's states
     recomputed with one-step fdtd2d_pass calls, then fdtd2d_adjoint_step
@@ -131,6 +131,7 @@ def _stepwise_gradient(pr):
     s._s.probe_ez = None
     seg, adj, tmp, ez = z(cp, len(names), nx, ny), z(len(names), nx, ny), z(nx, ny), z(nx, ny)
     grad = z(pr.box[2], pr.box[3])
+    gradn = z(pr.box[2], pr.box[3]) if with_nbz else None
     box = _lib.Box2D(*pr.box)
     st = _lib.stream_ptr()
     for c in reversed(range(ncp)):
@@ -142,8 +143,10 @@ def _stepwise_gradient(pr):
         for t in range(t0 + L, t0, -1):
             assert lib.fdtd2d_adjoint_step(t, C.byref(p), C.byref(fields(seg[t - t0 - 1])), C.byref(fields(adj)),
                                            tmp.data_ptr(), pr.probe[0], pr.probe[1], 2.0, box, grad.data_ptr(),
-                                           None, st) == 0
+                                           gradn.data_ptr() if with_nbz else None, st) == 0
     torch.cuda.synchronize()
+    if with_nbz:
+        return float((trace.double() ** 2).sum()), trace, grad, gradn
     return float((trace.double() ** 2).sum()), trace, grad
 
 
@@ -185,3 +188,36 @@ def test_one_call_adjoint_single_entry(cuda_lib):
     assert float(Jd.item()) == J
     assert torch.equal(g1, g)
     assert float(gn.abs().max()) > 0  # dJ/dnbz over the lossy box
+
+
+@pytest.mark.parametrize("nx,ny,box,off,sigma,cp,kind", [
+    (100, 132, (32, 32), 20, 0.05, 21, "soft"),   # no dimension a multiple of the 16 x 32 reverse tile
+    (72, 100, (16, 16), 15, 0.0, 9, "hard"),      # lossless box, hard source, odd segments
+    (144, 96, (32, 32), 10, 0.05, 10, "hard"),    # even segments only: every reverse launch takes two steps
+])
+def test_two_step_reverse_equals_stepwise(cuda_lib, nx, ny, box, off, sigma, cp, kind):
+    """The reverse sweep (two steps per launch, one for an odd segment's first
+    step) gives dJ/dnaz and dJ/dnbz bit for bit equal to one two-kernel
+    fdtd2d_adjoint_step per step, on grids that are not multiples of the
+    reverse tile, with hard and soft sources, lossless and lossy boxes."""
+    import ctypes as C
+    from simulation_gb300 import _lib
+    from simulation_gb300 import adjoint as A
+    pr = A.AdjointProblem(nx=nx, ny=ny, npml=8, box=box, src_offset=off, probe_offset=off, ns=220, checkpoint=cp,
+                          wave=("gauss", 30, 8.0), src_kind=kind, sigma_box=sigma)
+    pr.use_graphs = False
+    eps = torch.as_tensor(np.random.default_rng(5).uniform(1, 4, size=box), dtype=torch.float64)
+    pr.set_eps(eps)
+    pr.forward()
+    lossy = sigma > 0
+    g = torch.zeros(box, dtype=torch.float32, device="cuda")
+    gn = torch.zeros_like(g)
+    _lib.call("fdtd2d_tm_adjoint_reverse", C.byref(pr.sim._p), C.byref(pr.ap), g.data_ptr(),
+              gn.data_ptr() if lossy else None, pr.ws.data_ptr(), pr.ws.numel(), _lib.stream_ptr())
+    torch.cuda.synchronize()
+    ref = _stepwise_gradient(pr, with_nbz=lossy)
+    assert torch.equal(g, ref[2])
+    assert float(g.abs().max()) > 0
+    if lossy:
+        assert torch.equal(gn, ref[3])
+        assert float(gn.abs().max()) > 0
