@@ -146,6 +146,22 @@ def plan(ke: np.ndarray, cpt: int, block: int) -> np.ndarray:
     return out
 
 
+# Source and DFT tables on the device, shared by every runner with the same
+# wave, frequencies, step count and device (read-only once built): building
+# them takes the host longer than a judge's FDTD batch takes to enqueue.
+_TABLES: dict = {}
+
+
+def _step_tables(wave, freqs: np.ndarray, nsteps: int, dev: torch.device):
+    key = (tuple(wave), freqs.tobytes(), nsteps, str(dev))
+    t = _TABLES.get(key)
+    if t is None:
+        cs, sn = dft_tables(freqs, DT, 1, nsteps)
+        t = (to_device(wave_values(wave, 1, nsteps), dev), to_device(cs, dev), to_device(sn, dev))
+        _TABLES[key] = t  # kept for the process: kernels on any stream may still read them
+    return t
+
+
 class BatchRunner:
     """Device-resident inputs of one batch and the launch(es) that run it."""
 
@@ -167,9 +183,7 @@ class BatchRunner:
         lca, lcb = layer_coeffs(batch.epsr, batch.sigma) if batch.epsr.size else (np.ones(1), np.ones(1))
         self.layer_ca, self.layer_cb = to_device(lca, dev), to_device(lcb, dev)
         self.probe_in, self.probe_out = i32(batch.probe_in), i32(batch.probe_out)
-        self.src_table = to_device(wave_values(wave, 1, nsteps), dev)
-        cs, sn = dft_tables(self.freqs, DT, 1, nsteps)
-        self.dft_cos, self.dft_sin = to_device(cs, dev), to_device(sn, dev)
+        self.src_table, self.dft_cos, self.dft_sin = _step_tables(wave, self.freqs, nsteps, dev)
         self.spec = torch.zeros((batch.nruns, 4, nf), dtype=torch.float32, device=dev)
         self.done = torch.zeros(batch.nruns, dtype=torch.int32, device=dev)
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)

@@ -555,9 +555,10 @@ class JudgedSurrogate:
     network and are solved by FDTD directly.
 
     Everything stays on the device: the inputs are built there from the layer
-    tables (``device_features``), and the FDTD runs of the spot check (and of
-    the gated profiles) are enqueued on a second stream before the network
-    runs, so the two overlap; the replacement waits for both."""
+    tables (``device_features``).  The network is enqueued first; the FDTD
+    runs of the spot check (and of the gated profiles) are then prepared on
+    the host while it runs and enqueued on a second stream, so the two
+    overlap; the replacement waits for both."""
 
     def __init__(self, model: FNO, check_frac: float = 0.01, tol: float = 0.01, nsteps: int = NSTEPS, seed: int = 0,
                  gate: tuple | None = None):
@@ -581,20 +582,20 @@ class JudgedSurrogate:
             self._side = torch.cuda.Stream(device=dev)
         side = self._side
         side.wait_stream(main)
-        ref = fall = None
-        with torch.cuda.stream(side):  # the judge's FDTD, overlapping the network below
-            if idx.size:
-                ref = solve_fdtd_device(batch.subset(idx), self.nsteps, device=dev)
-            if routed_idx.size:
-                fall = solve_fdtd_device(batch.subset(routed_idx), self.nsteps, device=dev)
         pred = torch.zeros((n, OUT), dtype=torch.float32, device=dev)
-        if served.size:
+        if served.size:  # the network, enqueued first: the GPU runs it while the host prepares the judge
             sv = torch.as_tensor(served, device=dev)
             if inp is None:
                 x = device_features(batch, served, nbins=self.model.N, device=dev)
             else:
                 x = inp.index_select(0, sv).contiguous()
             pred.index_copy_(0, sv, self.model.spectrum(x))
+        ref = fall = None
+        with torch.cuda.stream(side):  # the judge's FDTD, overlapping the network
+            if idx.size:
+                ref = solve_fdtd_device(batch.subset(idx), self.nsteps, device=dev)
+            if routed_idx.size:
+                fall = solve_fdtd_device(batch.subset(routed_idx), self.nsteps, device=dev)
         main.wait_stream(side)
         for t in (ref, fall):
             if t is not None:
