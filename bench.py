@@ -655,6 +655,27 @@ def _bench_surrogate(st, fdtd_spectra_per_s: float | None, n: int = 65536) -> di
     return res
 
 
+def host_link_gbps(host_src, dev_buf, host_dst, reps: int = 3) -> dict:
+    """Pinned host <-> device copy rate (GB/s) of one field array, each
+    direction alone, best of ``reps``: what the pipeline fill (the first
+    request's upload) and drain (the last one's download) run at."""
+    import torch
+    st = torch.cuda.current_stream()
+    out = {}
+    for name, dst, src in (("h2d", dev_buf, host_src), ("d2h", host_dst, dev_buf)):
+        best = None
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            dst.copy_(src, non_blocking=True)
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        out[name] = src.numel() * 4 / (best / 1e3) / 1e9 if best else None
+    return out
+
+
 def run_e2e(sim, args, st, world, dev) -> dict:
     """Same runs through SimTM2D with host (pinned) buffers copied in and out.
 
@@ -726,6 +747,7 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     for k in range(2):  # warm-up: workspaces, tables
         done = one(k, done)
     torch.cuda.synchronize()
+    link = host_link_gbps(host_in["dz"], sims[0].dz, host_out[0]["dz"])
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
     for x in up + comp + down:
@@ -747,7 +769,9 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     ms = max_over_ranks(ms, world, dev)
     return {"value": whole_job_rate(NX * NY * NS * steps, world, ms), "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms / steps, "steps": steps,
-            "simulations_in_flight": 2, "copy_streams": "upload and download per simulation"}
+            "simulations_in_flight": 2, "copy_streams": "upload and download per simulation",
+            "host_link_GBps": link,
+            "fill_drain_ms": (h2d / link["h2d"] + d2h / link["d2h"]) / 1e6 if link["h2d"] and link["d2h"] else None}
 
 
 def main():

@@ -511,9 +511,9 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe,
       }
       const float hx_left = __shfl_up_sync(FULL, in_hx[CPL - 1], 1);
       const bool drow = (q >= 1) && (q < nx);
-      bool d_tf = false;  // inctdz row (warp-uniform)
+      bool d_tf = false;  // inctdz row (warp-uniform); the interior form meets no TF/SF edge
       float hxi_lo = 0.f, hxi_hi = 0.f;
-      if (TFS) {
+      if (TFS && !INT) {
         d_tf = q >= np - 1 && q <= nx - np;
         hxi_lo = __ldg(a.ext.inc_h + 2 * s);
         hxi_hi = __ldg(a.ext.inc_h + 2 * s + 1);
@@ -588,7 +588,7 @@ __device__ __forceinline__ void march_body(const MarchArgs& a, const int stripe,
       float ezr[CPL];
 #pragma unroll
       for (int c = 0; c < CPL; ++c) ezr[c] = 0.f;
-      if (TFS) {
+      if (TFS && !INT) {
         const float* erow = a.ext.inc_e + (size_t)s * ny;
         hx_tf = qc >= np - 1 && qc <= nx - np;
         ezi_lo = __ldg(erow + max(np - 1, 0));
