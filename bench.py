@@ -729,11 +729,14 @@ def run_e2e(sim, args, st, world, dev) -> dict:
             comp[i].wait_event(inputs)
             if prev_done is not None:
                 comp[i].wait_event(prev_done)  # compute after the previous step's compute
+            begin = torch.cuda.Event(enable_timing=True)
+            begin.record(comp[i])
             s.t = 0
             s.step(NS)
-            done = torch.cuda.Event()
+            done = torch.cuda.Event(enable_timing=True)
             done.record(comp[i])
             last_compute[i] = done
+            spans.append((begin, done))
         with torch.cuda.stream(down[i]):
             down[i].wait_event(done)
             for key in keys_out:
@@ -743,6 +746,7 @@ def run_e2e(sim, args, st, world, dev) -> dict:
                 out_done[i][key] = ev
         return done
 
+    spans = []  # (begin, end) events of each step's compute
     done = None
     for k in range(2):  # warm-up: workspaces, tables
         done = one(k, done)
@@ -754,6 +758,7 @@ def run_e2e(sim, args, st, world, dev) -> dict:
         x.wait_stream(st)
     done = None
     steps = max(args.steps, E2E_MIN_STEPS)
+    spans.clear()
     for k in range(steps):
         done = one(k, done)
     for x in up + comp + down:
@@ -761,6 +766,7 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     e1.record(st)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
+    compute_ms = statistics.median(b.elapsed_time(d) for b, d in spans)
     for s in sims:
         s.check()
     h2d = sum(v.numel() * 4 for v in host_in.values()) + sum(v.numel() * 4 for v in pml_host.values())
@@ -770,7 +776,7 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     return {"value": whole_job_rate(NX * NY * NS * steps, world, ms), "unit": UNIT,
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms / steps, "steps": steps,
             "simulations_in_flight": 2, "copy_streams": "upload and download per simulation",
-            "host_link_GBps": link,
+            "host_link_GBps": link, "compute_ms_per_step_median": compute_ms,
             "fill_drain_ms": (h2d / link["h2d"] + d2h / link["d2h"]) / 1e6 if link["h2d"] and link["d2h"] else None}
 
 
