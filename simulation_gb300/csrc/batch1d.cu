@@ -56,6 +56,22 @@ __device__ __forceinline__ void team_sync(int bar_id, int nthreads) {
   }
 }
 
+// a[c] for a runtime c (a select per cell: callers keep it to one thread)
+template <int CPT>
+__device__ __forceinline__ float cell_get(const float (&a)[CPT], int c) {
+  float r = 0.f;
+#pragma unroll
+  for (int k = 0; k < CPT; ++k)
+    if (k == c) r = a[k];
+  return r;
+}
+template <int CPT>
+__device__ __forceinline__ void cell_set(float (&a)[CPT], int c, float v) {
+#pragma unroll
+  for (int k = 0; k < CPT; ++k)
+    if (k == c) a[k] = v;
+}
+
 template <int CPT>
 __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id, int warp_base, float2* coef,
                          float* x_last_hy, float* x_first_ex, float* x_last_ex, float* x_probe, float* acc) {
@@ -64,16 +80,17 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
   const int w = tt >> 5;              // warp index inside the team
   const int nw = T >> 5;
   const int nx = p.ke[run];
-  const int g0 = tt * CPT;
 
-  // expand the layer table: background ca=1, cb=0.5 (free space of fd1d_1_5).
+  // expand the layer table: background ca=1, cb=0.5 (free space of fd1d_1_5);
+  // cells past the run's end get ca=cb=0, which keeps them exactly 0, so the
+  // cell loops below need no range test (their H update adds 0.5*(0-0)).
   // Cell c of thread (warp w, lane l) is stored at coef[(w*CPT + c)*32 + l]:
   // the warp's read of its c-th cells touches 32 consecutive float2 (a
   // thread-major layout puts lanes CPT*8 bytes apart: 8-way bank conflicts),
   // and each thread reads at constant offsets c*256 bytes from its own base.
   const int l0 = p.layer_off[run], l1 = p.layer_off[run + 1];
   for (int i = tt; i < T * CPT; i += T) {
-    float ca = 1.f, cb = 0.5f;
+    float ca = i < nx ? 1.f : 0.f, cb = i < nx ? 0.5f : 0.f;
     for (int l = l0; l < l1; ++l)
       if (i >= p.layer_start[l] && i < p.layer_end[l]) {
         ca = p.layer_ca[l];
@@ -96,6 +113,9 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
   const int hi_thr = (nx - 1) / CPT;
   const int hi_c = (nx - 1) - hi_thr * CPT;
   const bool own_hi = (tt == hi_thr);
+  // the threads (and their cells) holding the source and the two probes
+  const bool own_src = tt == p.src_k / CPT, own_pin = tt == pin / CPT, own_pout = tt == pout / CPT;
+  const int src_c = p.src_k % CPT, pin_c = pin % CPT, pout_c = pout % CPT;
   float bc0 = 0.f, bc1 = 0.f, bc2 = 0.f, bc3 = 0.f;
   if (lane == 31) x_last_hy[warp_base + w] = 0.f;
   team_sync(bar_id, T);
@@ -113,18 +133,18 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
     // ---------------- E stage: ex = ca*ex + cb*(hy[i-1]-hy[i])
     float hy_left = __shfl_up_sync(FULL, hy[CPT - 1], 1);
     if (lane == 0) hy_left = (w > 0) ? x_last_hy[warp_base + w - 1] : 0.f;
+    const float ex0 = ex[0];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
-      const int g = g0 + c;
       const float hym = (c == 0) ? hy_left : hy[c - 1];
-      if (g >= 1 && g < nx) {
-        const float2 k = my_coef[c * 32];
-        ex[c] = ex_update_cacb(ex[c], hym, hy[c], k.x, k.y);
-      }
-      if (g == p.src_k) ex[c] = __fadd_rn(ex[c], v);  // soft source, fd1d/program/fd1d_1_5.py:67
-      if (g == pin) x_probe[0] = ex[c];
-      if (g == pout) x_probe[1] = ex[c];
+      const float2 k = my_coef[c * 32];
+      ex[c] = ex_update_cacb(ex[c], hym, hy[c], k.x, k.y);
     }
+    if (own_lo) ex[0] = ex0;  // cell 0 is not E-updated
+    // soft source, fd1d/program/fd1d_1_5.py:67, then the probes read their cells
+    if (own_src) cell_set<CPT>(ex, src_c, __fadd_rn(cell_get<CPT>(ex, src_c), v));
+    if (own_pin) x_probe[0] = cell_get<CPT>(ex, pin_c);
+    if (own_pout) x_probe[1] = cell_get<CPT>(ex, pout_c);
     // ABC (fd1d/program/fd1d_1_2.py:47-48): low side here, high side's
     // ex[nx-1] here and its state shift after barrier A
     if (own_lo) {
@@ -133,11 +153,7 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
       bc0 = bc1;
       bc1 = e1;
     }
-    if (own_hi) {
-#pragma unroll
-      for (int c = 0; c < CPT; ++c)
-        if (c == hi_c) ex[c] = bc3;
-    }
+    if (own_hi) cell_set<CPT>(ex, hi_c, bc3);
     const float prev_last_ex = __shfl_up_sync(FULL, ex[CPT - 1], 1);
     if (lane == 0) x_first_ex[warp_base + w] = ex[0];
     if (lane == 31) x_last_ex[warp_base + w] = ex[CPT - 1];
@@ -157,25 +173,19 @@ __device__ void run_team(const BatchArgs& A, int run, int T, int tt, int bar_id,
         }
       }
     }
+    float hy_hi = 0.f;  // hy[nx-1] is never updated: kept across the unmasked H loop
     if (own_hi) {
-      float e_nm2 = 0.f;
-      if (hi_c >= 1) {
-#pragma unroll
-        for (int c = 1; c < CPT; ++c)
-          if (c == hi_c) e_nm2 = ex[c - 1];
-      } else {
-        e_nm2 = (lane > 0) ? prev_last_ex : x_last_ex[warp_base + w - 1];
-      }
+      const float e_nm2 = hi_c >= 1 ? cell_get<CPT>(ex, hi_c - 1)
+                                    : ((lane > 0) ? prev_last_ex : x_last_ex[warp_base + w - 1]);
       bc3 = bc2;
       bc2 = e_nm2;
+      hy_hi = cell_get<CPT>(hy, hi_c);
     }
     float ex_right = __shfl_down_sync(FULL, ex[0], 1);
     if (lane == 31) ex_right = (w + 1 < nw) ? x_first_ex[warp_base + w + 1] : 0.f;
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) {
-      const int g = g0 + c;
-      if (g <= nx - 2) hy[c] = hy_update(hy[c], ex[c], (c == CPT - 1) ? ex_right : ex[c + 1]);
-    }
+    for (int c = 0; c < CPT; ++c) hy[c] = hy_update(hy[c], ex[c], (c == CPT - 1) ? ex_right : ex[c + 1]);
+    if (own_hi) cell_set<CPT>(hy, hi_c, hy_hi);
     if (lane == 31) x_last_hy[warp_base + w] = hy[CPT - 1];
     team_sync(bar_id, T);  // barrier B
   }

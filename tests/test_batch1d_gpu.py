@@ -69,3 +69,36 @@ def test_clock_budget_stops_cleanly(cuda_lib):
     r2.run()
     torch.cuda.synchronize()
     assert int(r2.done.sum()) == 20
+
+
+def test_runs_bitwise_equal_to_per_function_kernels(cuda_lib):
+    """Sampled runs of the batch, replayed one at a time through the 1D
+    per-function kernels (fdtd1d_efield / fdtd1d_fourier / fdtd1d_hfield: ca/cb
+    form, soft source, two-step-back ABC, DFT at the entry and exit probes),
+    give the same spectrum accumulators bit for bit (fd1d/program/fd1d_1_5.py
+    with the running DFT of fd1d/program/fd1d_2_2.py:65-71)."""
+    from simulation_gb300 import batch1d as B
+    from simulation_gb300 import fd1d as G
+    batch = B.slab_batch(256, seed=11)
+    ns = 1500
+    runner = B.BatchRunner(batch, nsteps=ns)
+    runner.run()
+    torch.cuda.synchronize()
+    spec = runner.spec.cpu()
+    # short, long and mid-length runs (the longest needs the widest team)
+    order = np.argsort(batch.ke)
+    for r in (int(order[0]), int(order[len(order) // 2]), int(order[-1])):
+        nx = int(batch.ke[r])
+        ca = np.ones(nx)
+        cb = np.full(nx, 0.5)
+        for l in range(batch.layer_off[r], batch.layer_off[r + 1]):
+            lca, lcb = B.layer_coeffs(batch.epsr[l:l + 1], batch.sigma[l:l + 1])
+            ca[batch.layer_start[l]:batch.layer_end[l]] = lca[0]
+            cb[batch.layer_start[l]:batch.layer_end[l]] = lcb[0]
+        sim = G.Sim1D(nx, "cacb", ca=ca, cb=cb, src_kind="soft", src_k=int(batch.src_k), wave=("gauss", 50, 10.0),
+                      freq=runner.freqs, dt=B.DT, probes=(int(batch.probe_in[r]), int(batch.probe_out[r])), ns=ns)
+        sim.step_per_function(ns)
+        torch.cuda.synchronize()
+        got = spec[r]  # [4][nf]: re/im at the entry probe, re/im at the exit probe
+        want = torch.stack([sim.r_pr[0], sim.i_pr[0], sim.r_pr[1], sim.i_pr[1]]).cpu()
+        assert torch.equal(got, want), f"run {r} (ke={nx}): max {float((got - want).abs().max()):.3e}"
