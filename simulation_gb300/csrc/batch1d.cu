@@ -56,20 +56,27 @@ __device__ __forceinline__ void team_sync(int bar_id, int nthreads) {
   }
 }
 
-// a[c] for a runtime c (a select per cell: callers keep it to one thread)
+// a[c] for a runtime c: a switch (an indexed branch taken by the calling
+// lane), not a compare-and-select per cell; callers keep it to one thread
+#define FDTD_CELL_CASE(k)        \
+  case k:                        \
+    if constexpr (k < CPT) body(a[k < CPT ? k : 0]); \
+    break;
+template <int CPT, class A, class F>
+__device__ __forceinline__ void cell_at(A& a, int c, F&& body) {
+  static_assert(CPT <= 64, "cells per thread");
+  switch (c) { FDTD_CELL_CASE(0) FDTD_CELL_CASE(1) FDTD_CELL_CASE(2) FDTD_CELL_CASE(3) FDTD_CELL_CASE(4) FDTD_CELL_CASE(5) FDTD_CELL_CASE(6) FDTD_CELL_CASE(7) FDTD_CELL_CASE(8) FDTD_CELL_CASE(9) FDTD_CELL_CASE(10) FDTD_CELL_CASE(11) FDTD_CELL_CASE(12) FDTD_CELL_CASE(13) FDTD_CELL_CASE(14) FDTD_CELL_CASE(15) FDTD_CELL_CASE(16) FDTD_CELL_CASE(17) FDTD_CELL_CASE(18) FDTD_CELL_CASE(19) FDTD_CELL_CASE(20) FDTD_CELL_CASE(21) FDTD_CELL_CASE(22) FDTD_CELL_CASE(23) FDTD_CELL_CASE(24) FDTD_CELL_CASE(25) FDTD_CELL_CASE(26) FDTD_CELL_CASE(27) FDTD_CELL_CASE(28) FDTD_CELL_CASE(29) FDTD_CELL_CASE(30) FDTD_CELL_CASE(31) FDTD_CELL_CASE(32) FDTD_CELL_CASE(33) FDTD_CELL_CASE(34) FDTD_CELL_CASE(35) FDTD_CELL_CASE(36) FDTD_CELL_CASE(37) FDTD_CELL_CASE(38) FDTD_CELL_CASE(39) FDTD_CELL_CASE(40) FDTD_CELL_CASE(41) FDTD_CELL_CASE(42) FDTD_CELL_CASE(43) FDTD_CELL_CASE(44) FDTD_CELL_CASE(45) FDTD_CELL_CASE(46) FDTD_CELL_CASE(47) FDTD_CELL_CASE(48) FDTD_CELL_CASE(49) FDTD_CELL_CASE(50) FDTD_CELL_CASE(51) FDTD_CELL_CASE(52) FDTD_CELL_CASE(53) FDTD_CELL_CASE(54) FDTD_CELL_CASE(55) FDTD_CELL_CASE(56) FDTD_CELL_CASE(57) FDTD_CELL_CASE(58) FDTD_CELL_CASE(59) FDTD_CELL_CASE(60) FDTD_CELL_CASE(61) FDTD_CELL_CASE(62) FDTD_CELL_CASE(63) }
+}
+#undef FDTD_CELL_CASE
 template <int CPT>
 __device__ __forceinline__ float cell_get(const float (&a)[CPT], int c) {
   float r = 0.f;
-#pragma unroll
-  for (int k = 0; k < CPT; ++k)
-    if (k == c) r = a[k];
+  cell_at<CPT>(a, c, [&](const float& x) { r = x; });
   return r;
 }
 template <int CPT>
 __device__ __forceinline__ void cell_set(float (&a)[CPT], int c, float v) {
-#pragma unroll
-  for (int k = 0; k < CPT; ++k)
-    if (k == c) a[k] = v;
+  cell_at<CPT>(a, c, [&](float& x) { x = v; });
 }
 
 template <int CPT>
