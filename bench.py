@@ -766,7 +766,10 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     e1.record(st)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
-    compute_ms = statistics.median(b.elapsed_time(d) for b, d in spans)
+    compute_each = [b.elapsed_time(d) for b, d in spans]
+    compute_ms = statistics.median(compute_each)
+    # the gaps between one request's compute and the next (pipeline stalls)
+    gaps = [spans[k - 1][1].elapsed_time(spans[k][0]) for k in range(1, len(spans))]
     for s in sims:
         s.check()
     h2d = sum(v.numel() * 4 for v in host_in.values()) + sum(v.numel() * 4 for v in pml_host.values())
@@ -777,6 +780,7 @@ def run_e2e(sim, args, st, world, dev) -> dict:
             "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": ms / steps, "steps": steps,
             "simulations_in_flight": 2, "copy_streams": "upload and download per simulation",
             "host_link_GBps": link, "compute_ms_per_step_median": compute_ms,
+            "compute_ms_each": [round(x, 2) for x in compute_each], "gap_ms_each": [round(x, 2) for x in gaps],
             "fill_drain_ms": (h2d / link["h2d"] + d2h / link["d2h"]) / 1e6 if link["h2d"] and link["d2h"] else None}
 
 
