@@ -200,8 +200,9 @@ int fdtd2d_set_march_balance(float gen_cost);
  * when the driver reserves the array, so that first call can fail with
  * FDTD_ERR_CUDA if the device is out of memory; make it up front, before any
  * stream capture and before a memory budget is locked.  The address is kept
- * for the life of the process: calls after a cudaDeviceReset are not
- * supported.  All calls share the array (it keeps the
+ * per device and context: the first call in a new context (after a
+ * cudaDeviceReset, say) looks it up again, with the same caveat.  All calls
+ * share the array (it keeps the
  * last call's contents, none of which must start at zero); calls that overlap
  * on the GPU race on it.  With TF/SF or the DFT on and a workspace larger than
  * the array, each step is one fdtd2d_step_n call of one step instead. */

@@ -26,11 +26,14 @@
 //     cudaGetSymbolAddress; with lazy module loading that is when the driver
 //     reserves the array, so the first call can fail with FDTD_ERR_CUDA when
 //     the device is out of memory: make it up front, before any stream
-//     capture; the address is kept for the process (no cudaDeviceReset);
+//     capture; the address is kept per device and context, and looked up
+//     again when the current context is a new one (after a cudaDeviceReset);
 //   * all calls share the one array and it keeps the last call's contents;
 //     nothing in it has to start at zero (each call's first pass overwrites
 //     it before reading it), but calls whose work overlaps on the GPU (two
 //     streams, two host threads) race on it.
+#include <dlfcn.h>
+
 #include <mutex>
 
 #include "fdtd_common.cuh"
@@ -46,6 +49,31 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_addr[kMaxDevices] = {nullptr};
+unsigned long long g_ctx[kMaxDevices] = {0};  // the context the address belongs to (0: unknown)
+
+// Unique ID of the calling thread's current context (CUDA 12+ driver, found
+// in the driver library the runtime has already loaded; nothing is linked),
+// or 0 where it cannot be told.  A context created anew (after a
+// cudaDeviceReset, say) has a new ID, so the scratch address is looked up again.
+unsigned long long current_context_id() {
+  using GetCurrent = int (*)(void**);
+  using GetId = int (*)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* h = dlopen("libcuda.so.1", RTLD_NOW | RTLD_NOLOAD);
+    if (h) {
+      get_current = reinterpret_cast<GetCurrent>(dlsym(h, "cuCtxGetCurrent"));
+      get_id = reinterpret_cast<GetId>(dlsym(h, "cuCtxGetId"));
+    }
+  });
+  if (!get_current || !get_id) return 0;
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != 0 || ctx == nullptr || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 int scratch_address(void** out) {
   int dev = -1;
@@ -55,8 +83,9 @@ int scratch_address(void** out) {
     return FDTD_ERR_CUDA;
   }
   if (dev < 0 || dev >= kMaxDevices) return FDTD_ERR_UNSUPPORTED;
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_addr[dev]) {
+  if (!g_addr[dev] || (ctx != 0 && ctx != g_ctx[dev])) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) {
@@ -64,6 +93,7 @@ int scratch_address(void** out) {
       return FDTD_ERR_CUDA;
     }
     g_addr[dev] = p;
+    g_ctx[dev] = ctx;
   }
   *out = g_addr[dev];
   return FDTD_OK;
