@@ -443,6 +443,23 @@ def _bench_fd1d(st, reps: int = 20) -> dict:
     torch.cuda.synchronize()
     us = e0.elapsed_time(e1) * 1e3 / reps
     res = {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3, "kernel_launches_per_run": 1}
+    # the same run captured once in a CUDA graph and replayed (no host work per run)
+    g = torch.cuda.CUDAGraph()
+    cap = torch.cuda.Stream()
+    cap.wait_stream(st)
+    with torch.cuda.stream(cap):
+        with torch.cuda.graph(g, stream=cap):
+            sim.t = 0
+            sim.step(1000)
+    st.wait_stream(cap)
+    g.replay()
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        g.replay()
+    e1.record(st)
+    torch.cuda.synchronize()
+    res["us_per_run_graph"] = e0.elapsed_time(e1) * 1e3 / reps
     try:  # the same run through the reference's NumPy form (float64 restatement), one host thread
         from oracle import fd1d as O1
         kw = O1.program("config1")
