@@ -154,3 +154,16 @@ def test_probe_dft_more_frequencies_than_threads(cuda_lib, nx, nf):
     freq = np.linspace(5e7, 9e8, nf)
     _fused_vs_per_function(nx, "dform", 120, src_kind="soft", src_k=3, wave=("gauss", 20, 6.0), freq=freq,
                            probes=(1, nx // 3, nx - 2), full_dft=False)
+
+
+# the single-warp run without the DFT at 4, 8 and 16 cells per lane, nx a
+# multiple of them (the compile-time ABC variant): sources on either side of
+# a lane edge, odd step counts, with and without the ABC
+@pytest.mark.parametrize("nx,src_k", [(128, 3), (128, 4), (200, 7), (200, 8), (200, 9), (200, 15), (512, 16),
+                                      (512, 31), (512, 1)])
+@pytest.mark.parametrize("form", ["cb", "cacb"])
+def test_warp_kernel_lane_edge_sources_bitwise(cuda_lib, nx, src_k, form):
+    hard = src_k % 2 == 1
+    for ns, abc in ((301, True), (250, False)):
+        _fused_vs_per_function(nx, form, ns, src_kind="hard" if hard else "soft", src_k=src_k,
+                               wave=("gauss", 20, 6.0), abc=abc)
