@@ -749,6 +749,8 @@ def run_e2e(sim, args, st, world, dev) -> dict:
         with torch.cuda.stream(up[i]):
             if last_compute[i] is not None:
                 up[i].wait_event(last_compute[i])
+            u0 = torch.cuda.Event(enable_timing=True)
+            u0.record(up[i])
             for key in order_in:
                 ev = out_done[i].get(key)
                 if ev is not None:
@@ -756,8 +758,9 @@ def run_e2e(sim, args, st, world, dev) -> dict:
                 getattr(s, key).copy_(host_in[key], non_blocking=True)
             for key, v in pml_host.items():
                 getattr(s.pml, key).copy_(v, non_blocking=True)
-            inputs = torch.cuda.Event()
+            inputs = torch.cuda.Event(enable_timing=True)
             inputs.record(up[i])
+            uploads.append((u0, inputs))
         with torch.cuda.stream(comp[i]):
             comp[i].wait_event(inputs)
             if prev_done is not None:
@@ -772,19 +775,25 @@ def run_e2e(sim, args, st, world, dev) -> dict:
             spans.append((begin, done))
         with torch.cuda.stream(down[i]):
             down[i].wait_event(done)
+            d0 = torch.cuda.Event(enable_timing=True)
+            d0.record(down[i])
             for key in keys_out:
                 o[key].copy_(getattr(s, key), non_blocking=True)
-                ev = torch.cuda.Event()
+                ev = torch.cuda.Event(enable_timing=True)
                 ev.record(down[i])
                 out_done[i][key] = ev
+            downloads.append((d0, ev))
         return done
 
     spans = []  # (begin, end) events of each step's compute
+    uploads, downloads = [], []  # (begin, end) events of each step's copies
+    link = host_link_gbps(host_in["dz"], sims[0].dz, host_out[0]["dz"])
+    # warm-up requests, the last thing before the timed region: workspaces,
+    # tables, and every host buffer of both simulations recently copied
     done = None
-    for k in range(2):  # warm-up: workspaces, tables
+    for k in range(2):
         done = one(k, done)
     torch.cuda.synchronize()
-    link = host_link_gbps(host_in["dz"], sims[0].dz, host_out[0]["dz"])
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(st)
     for x in up + comp + down:
@@ -792,6 +801,8 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     done = None
     steps = max(args.steps, E2E_MIN_STEPS)
     spans.clear()
+    uploads.clear()
+    downloads.clear()
     for k in range(steps):
         done = one(k, done)
     for x in up + comp + down:
@@ -801,8 +812,10 @@ def run_e2e(sim, args, st, world, dev) -> dict:
     ms = e0.elapsed_time(e1)
     compute_each = [b.elapsed_time(d) for b, d in spans]
     compute_ms = statistics.median(compute_each)
-    # the gaps between one request's compute and the next (pipeline stalls)
+    # the gaps between one request's compute and the next (pipeline stalls),
+    # and the time before the first compute (fill) and after the last (drain)
     gaps = [spans[k - 1][1].elapsed_time(spans[k][0]) for k in range(1, len(spans))]
+    lead, tail = e0.elapsed_time(spans[0][0]), spans[-1][1].elapsed_time(e1)
     for s in sims:
         s.check()
     h2d = sum(v.numel() * 4 for v in host_in.values()) + sum(v.numel() * 4 for v in pml_host.values())
@@ -814,6 +827,9 @@ def run_e2e(sim, args, st, world, dev) -> dict:
             "simulations_in_flight": 2, "copy_streams": "upload and download per simulation",
             "host_link_GBps": link, "compute_ms_per_step_median": compute_ms,
             "compute_ms_each": [round(x, 2) for x in compute_each], "gap_ms_each": [round(x, 2) for x in gaps],
+            "fill_ms": lead, "drain_ms": tail,
+            "upload_ms_each": [round(a.elapsed_time(b), 2) for a, b in uploads],
+            "download_ms_each": [round(a.elapsed_time(b), 2) for a, b in downloads],
             "fill_drain_ms": (h2d / link["h2d"] + d2h / link["d2h"]) / 1e6 if link["h2d"] and link["d2h"] else None}
 
 
