@@ -167,3 +167,22 @@ def test_warp_kernel_lane_edge_sources_bitwise(cuda_lib, nx, src_k, form):
     for ns, abc in ((301, True), (250, False)):
         _fused_vs_per_function(nx, form, ns, src_kind="hard" if hard else "soft", src_k=src_k,
                                wave=("gauss", 20, 6.0), abc=abc)
+
+
+@pytest.mark.parametrize("nx", [200, 203, 700])
+def test_fused_split_calls_bitwise(cuda_lib, nx):
+    """One run as several fused calls (t0 > 0, not on the 32-step source
+    chunks of the single-warp kernel) equals the per-function loop: sources,
+    ABC state and the running DFT continue across calls."""
+    from simulation_gb300 import fd1d as G
+    co = _coeffs(nx, "dform")
+    kw = dict(src_kind="soft", src_k=3, wave=("gauss", 30, 8.0), freq=[1e8, 4e8], probes=(2, nx - 3),
+              full_dft=True, **co)
+    a, b = G.Sim1D(nx, "dform", **kw), G.Sim1D(nx, "dform", **kw)
+    for n in (37, 100, 1, 163):
+        a.step(n)
+    b.step_per_function(301)
+    torch.cuda.synchronize()
+    for k in ("ex", "hy", "dx", "ix", "bc", "r_pt", "i_pt", "r_pr", "i_pr"):
+        x, y = getattr(a, k), getattr(b, k)
+        assert torch.equal(x, y), f"nx={nx} {k}"
