@@ -442,7 +442,10 @@ def _bench_fd1d(st, reps: int = 20) -> dict:
     e1.record(st)
     torch.cuda.synchronize()
     us = e0.elapsed_time(e1) * 1e3 / reps
-    res = {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3, "kernel_launches_per_run": 1}
+    # 20 B per cell-update (ex, hy, cb read; ex, hy written) if it were streamed:
+    # the line lives in registers, and the run is bound by the step's latency
+    res = {"us_per_run": us, "Gcell_updates_per_s": 200 * 1000 / us / 1e3, "kernel_launches_per_run": 1,
+           "bytes_per_cell_update": 20, "GBps_algorithmic": 200 * 1000 * 20 / us / 1e3, "bound": "latency"}
     # the same run captured once in a CUDA graph and replayed (no host work per run)
     g = torch.cuda.CUDAGraph()
     cap = torch.cuda.Stream()
