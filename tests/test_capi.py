@@ -133,3 +133,55 @@ def test_workspace_size_host_arithmetic(lib):
     assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 0
     p.tfsf_npml = 0
     assert lib.fdtd2d_workspace_size(C.byref(p), 0) == 6 * ((100 * 16388 * 4 + 255) // 256 * 256)
+
+
+def test_adjoint_and_noalloc_argument_checks_without_gpu(lib):
+    """The one-call adjoint's workspace size is host arithmetic (checkpoint
+    states, pass ping-pong, two record buffers, adjoint ping-pong), and it and
+    the no-alloc step reject bad arguments before any CUDA call."""
+    from simulation_gb300 import _lib
+    fake = 0x10000  # never dereferenced
+    p = _lib.Params2D()
+    p.nx, p.ny = 64, 64
+    p.naz = fake
+    for k, _ in _lib.Pml2D._fields_:
+        setattr(p.pml, k, fake)
+    a = _lib.AdjointParams2D(100, 16, 40, 32, 2.0, _lib.Box2D(20, 20, 16, 16))
+    slot = (64 * 64 * 4 + 255) // 256 * 256
+    ncp = -(-100 // 16)
+    size = lib.fdtd2d_tm_adjoint_workspace_size
+    # lossless: 5 fields per state, 3 per record (dz, hx, hy)
+    assert size(C.byref(p), C.byref(a)) == slot * ((ncp + 1) * 5 + 2 * 5 + 1 + 2 * 15 * 3 + 2 * 5 + 1)
+    p.nbz = fake  # lossy: iz too
+    assert size(C.byref(p), C.byref(a)) == slot * ((ncp + 1) * 6 + 2 * 6 + 1 + 2 * 15 * 4 + 2 * 6 + 1)
+    bad = [("ny", 66), ("nsteps", 0), ("checkpoint", 0), ("probe_i", 64), ("tfsf_npml", 8), ("nf", 2)]
+    for name, v in bad:
+        obj = a if hasattr(a, name) else p
+        old = getattr(obj, name)
+        setattr(obj, name, v)
+        assert size(C.byref(p), C.byref(a)) == 0, name
+        setattr(obj, name, old)
+    a.box = _lib.Box2D(60, 20, 16, 16)  # past the grid
+    assert size(C.byref(p), C.byref(a)) == 0
+    a.box = _lib.Box2D(20, 20, 16, 16)
+    p.src.kind, p.src.i, p.src.j = 1, 30, 30  # a source needs its table, long enough
+    assert size(C.byref(p), C.byref(a)) == 0
+    p.src.table, p.src.table_len = fake, 99
+    assert size(C.byref(p), C.byref(a)) == 0
+    p.src.table_len = 100
+    n = size(C.byref(p), C.byref(a))
+    assert n > 0
+    fwd, rev = lib.fdtd2d_tm_adjoint_forward, lib.fdtd2d_tm_adjoint_reverse
+    assert fwd(C.byref(p), C.byref(a), None, None, fake, n, None) == -1  # no trace buffer
+    assert fwd(C.byref(p), C.byref(a), fake, None, None, n, None) == -9  # no workspace
+    assert fwd(C.byref(p), C.byref(a), fake, None, fake + 16, n, None) == -3  # workspace not 256-byte aligned
+    assert fwd(C.byref(p), C.byref(a), fake, None, fake, n - 1, None) == -9  # workspace too small
+    assert rev(C.byref(p), C.byref(a), None, None, fake, n, None) == -1  # no gradient buffer
+    p.nbz = None
+    assert rev(C.byref(p), C.byref(a), fake, fake, fake, n, None) == -4  # dJ/dnbz of a lossless box
+    # no-alloc step: bad step counts and grids past its static array
+    s = _lib.State2D()
+    assert lib.fdtd2d_step_n_noalloc(C.byref(p), C.byref(s), 0, -1, 0, None) == -4
+    assert lib.fdtd2d_step_n_noalloc(C.byref(p), C.byref(s), -1, 1, 0, None) == -4
+    p.nx, p.ny = 1025, 1024
+    assert lib.fdtd2d_step_n_noalloc(C.byref(p), C.byref(s), 0, 1, 0, None) == -2
